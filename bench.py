@@ -1,0 +1,325 @@
+"""Benchmark: solves/s of the MoM hot path (fill + LU + far field) on GB300.
+
+Workload (default): PEC sphere, level-4 icosphere (5120 triangles, N = 7680
+RWG), radius 1 m, seeded tangential jitter +-3% of the edge length, 450 MHz,
+x-polarised plane wave incident along -z, bistatic far field (sigma_VV,
+sigma_HH) at R = 10 m on 181 theta x 2 phi cuts. One step = one full solve:
+  fill Z -> plane-wave RHS -> LU + solve (mixed: complex64 LU + FP64
+  refinement against the FP64 Z) -> current lumping -> far-field sigma.
+Synthetic inputs (seeded mesh); the working set (Z: 0.94 GB c128 + 0.47 GB c64)
+is far larger than L2, so no extra flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+                  [--impl ours|reference]
+
+`--impl reference` times FRICO's CPU path on the host cores: the oracle
+(a restatement of FRICO's fill / lumping / fields with OpenMP) plus LAPACK
+zgetrf/zgetrs through scipy, each step a bounded sample (fill on a slice of
+the columns, scaled to the full matrix; full LU + solve; full fields).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+FREQ = 450e6
+R_FAR = 10.0
+WORKLOAD = "sphere_L4_N7680_450MHz_planewave_bistatic181x2"
+METRIC = "solves/s (fill+LU+far-field)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--level", type=int, default=4, help="icosphere level (4: N=7680)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, ws, rank, backend="gloo"):
+        self.ws, self.rank = ws, rank
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group(backend, rank=rank, world_size=ws)
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU paths
+def cpu_sample(mesh, steps: int, warmup: int, Zfull=None):
+    """FRICO's CPU path on a bounded sample; returns (sec/solve list, cores, sample desc)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+    from frico_gb300 import meshes
+    o = Oracle(mesh)
+    n = o.n
+    cols = max(64, n // 16)
+    if Zfull is None:
+        Zfull = o.compute_matrix(FREQ)
+    V = o.rhs_plane_wave(FREQ, 0.0, 0.0, 1.0, 0.0)
+    T, P, _ = meshes.bistatic_cuts(R_FAR)
+    times = []
+    for s in range(warmup + steps):
+        c0 = (s * cols) % max(1, n - cols)
+        t0 = time.perf_counter()
+        o.compute_matrix_cols(FREQ, c0, c0 + cols)
+        t_fill = (time.perf_counter() - t0) * (n / cols)
+        t1 = time.perf_counter()
+        V = o.rhs_plane_wave(FREQ, 0.0, 0.0, 1.0, 0.0)
+        I = o.solve(Zfull, V)
+        o.lump(FREQ, I)
+        o.rcs(R_FAR, T, P)
+        t_rest = time.perf_counter() - t1
+        if s >= warmup:
+            times.append(t_fill + t_rest)
+    sample = (f"per step: fill of {cols}/{n} columns (scaled x{n / cols:.1f}), full zgetrf+zgetrs (N={n}), "
+              f"lumping, 362-point far field")
+    return times, os.cpu_count(), sample
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from frico_gb300 import meshes
+    mesh = meshes.icosphere(args.level)
+    times, cores, sample = cpu_sample(mesh, args.steps, args.warmup)
+    t = sum(times)
+    value = len(times) / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded icosphere)", "config": {"workload": WORKLOAD, "precision": "fp64 (LAPACK)"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU path
+def run_ours(args):
+    ws, rank, local = dist_env()
+    dist = Dist(ws, rank)
+    import ctypes as C
+    import frico_gb300
+    frico_gb300.build()
+    from frico_gb300 import _abi, meshes
+    from frico_gb300.solver import PlaneWave, Simulation
+
+    mesh = meshes.icosphere(args.level)
+    T, P, _ = meshes.bistatic_cuts(R_FAR)
+    sim = Simulation(mesh, precision=args.precision, device=local, profile_kernels=True)
+    lib = sim.lib
+    n = sim.n
+    pw = PlaneWave(0.0, 0.0, 1.0, 0.0)
+    stream = C.c_void_p()
+    lib.frico_gpu_get_stream(sim.ctx, C.byref(stream))
+    import torch
+    torch.cuda.set_device(local)
+    ext = torch.cuda.ExternalStream(stream.value, device=local)
+
+    def step():
+        sim.compute_matrix(FREQ)
+        sim.set_nrhs(1)
+        sim.update_rhs(FREQ, pw)
+        sim.solve(download=False)
+        return sim.rcs_points(R_FAR, T, P)
+
+    for _ in range(args.warmup):
+        step()
+    s0 = sim.stats()
+    clocks = ClockSampler(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    stage = {k: 0.0 for k in ("fill_ms", "rhs_ms", "factor_ms", "solve_ms", "refine_ms", "fields_ms")}
+    iters = []
+    for _ in range(args.steps):
+        sig = step()
+        st = sim.stats()
+        for k in stage:
+            stage[k] += st[k]
+        iters.append(st["refine_iters"])
+    e1.record(ext)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    dist.barrier()
+    clk = clocks.stop()
+    s1 = sim.stats()
+    ms_max = dist.max(ms)
+    value = ws * args.steps / (ms_max / 1000.0)
+
+    # -- end to end through the C-ABI with host buffers (mesh in, currents + sigma out)
+    fs = sim.fs
+    I_host = np.empty((n, 1), np.complex128, order="F")
+    th = np.ascontiguousarray(T)
+    ph = np.ascontiguousarray(P)
+    sig_host = np.empty((T.shape[0], 2))
+    info = C.c_int32(0)
+    h2d = fs.vertices.nbytes + fs.triangles.nbytes + fs.rwg.nbytes + 3 * 8 * T.shape[0]
+    d2h = I_host.nbytes + 3 * 16 * T.shape[0]
+
+    def e2e_step():
+        sim._call("frico_gpu_set_mesh", fs.vertices.shape[0], _abi.ptr(fs.vertices), fs.triangles.shape[0],
+                  _abi.ptr(fs.triangles), n, _abi.ptr(fs.rwg))
+        sim._call("frico_gpu_fill", FREQ, None, n)
+        sim._call("frico_gpu_set_nrhs", 1)
+        sim._call("frico_gpu_rhs_plane_wave", FREQ, 0, 0.0, 0.0, _abi.C128(1.0, 0.0), _abi.C128(0.0, 0.0))
+        sim._call("frico_gpu_solve", _abi.ptr(I_host), n, C.byref(info))
+        sim._call("frico_gpu_rcs_points", 0, R_FAR, T.shape[0], _abi.ptr(th), _abi.ptr(ph), _abi.ptr(sig_host))
+
+    e2e_step()
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = ws * args.steps / e2e_s
+
+    # -- roofline of the dominant kernel: LU trailing-update GEMM
+    gl = s1["gemm_launches"] - s0["gemm_launches"]
+    gms = s1["gemm_ms"] - s0["gemm_ms"]
+    gfl = s1["gemm_flops"] - s0["gemm_flops"]
+    hbm, bf16, peak_src = measured_peaks()
+    achieved = gfl / (gms / 1000.0) / 1e12 if gms > 0 else 0.0
+    roof = {"kernel": "k_gemm_update<float>" if args.precision == "mixed" else "k_gemm_update<double>",
+            "bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+            "frac": achieved / bf16, "traffic": None, "launches_per_step": gl / args.steps,
+            "avg_launch_us": 1000.0 * gms / max(1, gl),
+            "note": f"SIMT complex GEMM (no tensor cores yet); peak = dense bf16 ({peak_src})"}
+
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64+c128" if args.precision == "mixed" else "c128",
+            "data": "synthetic (seeded icosphere L%d)" % args.level,
+            "config": {"workload": WORKLOAD.replace("L4_N7680", f"L{args.level}_N{n}"), "n": n, "ntri": sim.nt,
+                       "precision": args.precision, "rhs": 1, "far_field_points": int(T.shape[0]),
+                       "l2": "working set > L2 (Z 0.94 GB)", "replicas": ws},
+            "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+            "refine_iters": iters[-1] if iters else 0,
+            "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": roof, "clocks": clk}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        Zfull = sim.compute_matrix(FREQ, download=True)
+        times, cores, sample = cpu_sample(mesh, 1, 0, Zfull)
+        line["cpu_baseline"] = {"value": 1.0 / times[0], "unit": "solves/s", "cores": cores, "kind": "port",
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    dist.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,14 @@
+"""GB300 (sm_103a) implementation of FRICO's Method-of-Moments hot path.
+
+The compute lives in libfrico_gpu.so (include/frico_gpu.h); this package is the
+host-side mirror of FRICO's solver interface plus the synthetic workloads.
+"""
+from . import meshes  # noqa: F401
+from ._abi import FricoError  # noqa: F401
+
+__all__ = ["meshes", "FricoError", "build", "solver"]
+
+
+def build(verbose: bool = False, force: bool = False):
+    from .build import build as _b
+    return _b(verbose=verbose, force=force)

@@ -1,0 +1,178 @@
+// Internal definitions shared by the CUDA translation units of libfrico_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "frico_gpu.h"
+
+// src/constants.h:24-25
+#define FRICO_MU0 1.256637061435917e-06
+#define FRICO_EPS0 8.8541878188e-12
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+#ifndef M_1_PI
+#define M_1_PI 0.31830988618379067154
+#endif
+
+namespace frico {
+
+// ---------------------------------------------------------------- complex
+template <typename R> struct cvec;
+template <> struct cvec<double> { using type = double2; };
+template <> struct cvec<float> { using type = float2; };
+template <typename R> using cplx = typename cvec<R>::type;
+
+__host__ __device__ __forceinline__ double2 cmake(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ float2 cmake(float r, float i) { return make_float2(r, i); }
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return {a.x + b.x, a.y + b.y}; }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return {a.x - b.x, a.y - b.y}; }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) { return {a.x * s, a.y * s}; }
+// a - b*c
+template <typename C> __host__ __device__ __forceinline__ C cfms(C a, C b, C c) {
+    return {a.x - b.x * c.x + b.y * c.y, a.y - b.x * c.y - b.y * c.x};
+}
+// Complex division a / b as std::complex<double> operator/ computes it in the
+// common case (Smith-free textbook form; the inputs here are well scaled).
+template <typename C> __host__ __device__ __forceinline__ C cdiv(C a, C b) {
+    auto d = b.x * b.x + b.y * b.y;
+    return {(a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d};
+}
+template <typename C> __host__ __device__ __forceinline__ auto cabs1(C a) { return fabs(a.x) + fabs(a.y); }
+
+// ---------------------------------------------------------------- errors
+#define FRICO_DEV_ERR_TIMEOUT 1
+#define FRICO_DEV_ERR_BOUNDS 2
+
+struct DeviceStatus {
+    int err;       // FRICO_DEV_ERR_* (first one wins)
+    int info;      // LAPACK-style info of the last factorisation (0 = ok)
+    int where;     // diagnostic: which barrier / index gave up
+    int pad;
+};
+
+// ---------------------------------------------------------------- mesh on device
+// Per-triangle geometry, 16 doubles: v0, v1, v2, barycentre, area (cross
+// product, src/geom_mesh.cpp:71-78), Kahan area (src/quadratures.cpp:41-57), pad.
+struct TriGeo {
+    double v[9];
+    double c[3];
+    double area;
+    double area_kahan;
+    double pad[2];
+};
+
+// Device-side RWG table in structure-of-arrays form.
+struct RwgDev {
+    int32_t* itm;   // T- index
+    int32_t* itp;   // T+ index
+    double* len;    // edge length
+    double* am;     // area T-
+    double* ap;     // area T+
+    double* vm;     // free vertex of T-  [3n]
+    double* vp;     // free vertex of T+  [3n]
+    int32_t* itf;   // interface tag or INT32_MIN
+};
+
+struct Ctx;
+
+// Workspace that only grows; freed with the context.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace frico
+
+struct frico_gpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    frico_gpu_options opt{};
+    std::string last_error;
+
+    // mesh
+    int64_t nv = 0, nt = 0, n = 0;
+    int geo_degree = -1;          // degree the quadrature tables were built for
+    int nq = 0;                   // points per triangle at that degree
+    frico::DevBuf xyz, tri, trigeo, qp, qps, rwg_itm, rwg_itp, rwg_len, rwg_am, rwg_ap, rwg_vm,
+        rwg_vp, rwg_itf;
+    frico::DevBuf tri_bf;         // [nt*3] basis index (+1, signed by side) per triangle slot
+    std::vector<frico_rwg> h_rwg; // host copy (port values, interfaces)
+
+    // fill
+    double freq = 0.0;
+    bool z_valid = false;         // Z64 holds the matrix of `freq`
+    frico::DevBuf gtab, smom, basis_aux, z64, z32;
+
+    // factorisation / solve
+    bool factored = false;
+    int factor_prec = -1;
+    int32_t info = 0;
+    frico::DevBuf lu, ipiv, perm, panel_ws, status;
+    int32_t nrhs = 0;
+    frico::DevBuf rhs, sol, rwork, rwork32, dwork32, norms;
+    bool solved = false;
+
+    // post-processing
+    frico::DevBuf tri_aj, tri_adivj, tri_j, fld_pts, fld_part, fld_out;
+    int32_t lumped_col = -1;
+
+    frico_gpu_stats stats{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> prof_events;   // pairs around profiled launches
+    size_t prof_used = 0;
+};
+
+namespace frico {
+
+// Returns FRICO_GPU_OK or sets ctx->last_error and returns a code.
+int set_err(frico_gpu_ctx* ctx, int code, const std::string& msg);
+int cuda_check(frico_gpu_ctx* ctx, cudaError_t e, const char* what);
+int ensure(frico_gpu_ctx* ctx, DevBuf& b, size_t bytes);
+void release(DevBuf& b);
+
+// Stage timing on the context stream.
+struct StageTimer {
+    frico_gpu_ctx* ctx;
+    double* out;
+    StageTimer(frico_gpu_ctx* c, double* o) : ctx(c), out(o) { cudaEventRecord(ctx->ev0, ctx->stream); }
+    ~StageTimer() {
+        cudaEventRecord(ctx->ev1, ctx->stream);
+        if (cudaEventSynchronize(ctx->ev1) == cudaSuccess) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+            *out = ms;
+        }
+    }
+};
+
+// Count one kernel launch on the context (reported as stats.kernel_launches).
+inline void count_launch(frico_gpu_ctx* ctx, int64_t k = 1) { ctx->stats.kernel_launches += k; }
+
+// ---- kernels' host launchers (defined in the .cu files) ----
+int build_quadrature(frico_gpu_ctx* ctx);                     // fill.cu
+int fill_matrix(frico_gpu_ctx* ctx, double freq);             // fill.cu
+int symmetrize(frico_gpu_ctx* ctx);                           // fill.cu
+int lu_factor_fp64(frico_gpu_ctx* ctx);                       // lu.cu
+int lu_factor_fp32(frico_gpu_ctx* ctx);                       // lu.cu
+int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb);   // lu.cu
+int lu_solve_fp32(frico_gpu_ctx* ctx, float2* B, int nrhs, int64_t ldb);    // lu.cu
+int refine_solve(frico_gpu_ctx* ctx);                         // lu.cu
+int rhs_delta_gap(frico_gpu_ctx* ctx, double freq, int col, int n_itf, const int32_t* tags,
+                  double2 V0, const double* signs);           // fields.cu
+int rhs_plane_wave(frico_gpu_ctx* ctx, double freq, int col, double theta, double phi,
+                   double2 Eth, double2 Eph);                 // fields.cu
+int lump_currents(frico_gpu_ctx* ctx, int col);               // fields.cu
+int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_host,
+                    double2* E_host, double2* H_host);        // fields.cu
+
+}  // namespace frico

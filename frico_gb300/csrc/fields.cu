@@ -1,0 +1,316 @@
+// Right-hand sides, current lumping and field evaluation.
+//
+//   update_rhs(delta_gap)   src/emw_solver.cpp:352-378
+//   update_rhs(plane_wave)  src/emw_solver.cpp:380-416, plane_wave src/sources.h:34-75
+//   run_context lumping     src/emw_solver.h:137-164
+//   eval_fields             src/emw_postpro_common.cpp:31-66 (finite-R, exact
+//                           free-space kernel; H with exp(+jkR) in compat mode)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace frico {
+
+// V[i] += (-j l_i / (omega mu0)) * V0 * sign_i on RWGs whose interface tag is listed.
+__global__ void k_rhs_delta_gap(int64_t n, const int32_t* __restrict__ itf, const double* __restrict__ len,
+                                double omega, const int32_t* __restrict__ tags, int ntags, double2 V0,
+                                const double* __restrict__ signs, double2* __restrict__ V) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    int32_t t = itf[i];
+    if (t == INT32_MIN) return;
+    double2 acc = V[i];
+    for (int k = 0; k < ntags; k++)
+        if (t == tags[k]) {
+            double2 v = make_double2(0.0, -len[i] / (omega * FRICO_MU0));
+            double sign = signs ? signs[i] : 1.0;
+            double2 vv = cmul(v, V0);
+            acc = cadd(acc, make_double2(vv.x * sign, vv.y * sign));
+        }
+    V[i] = acc;
+}
+
+struct PlaneWave {
+    double dir[3], th[3], ph[3];
+    double2 Eth, Eph;
+};
+
+// E(q) = (Eth th + Eph ph) exp(j k dir.q)
+__device__ __forceinline__ void pw_field(const PlaneWave& pw, double k, const double* q, double2* E) {
+    double d = pw.dir[0] * q[0] + pw.dir[1] * q[1] + pw.dir[2] * q[2];
+    double s, c;
+    sincos(k * d, &s, &c);
+    double2 ph = make_double2(c, s);
+    for (int a = 0; a < 3; a++) {
+        double2 e0 = cadd(cscale(pw.Eth, pw.th[a]), cscale(pw.Eph, pw.ph[a]));
+        E[a] = cmul(e0, ph);
+    }
+}
+
+__global__ void k_rhs_plane_wave(int64_t n, RwgDev rw, const double* __restrict__ qp, int nq, double k,
+                                 double omega, PlaneWave pw, double2* __restrict__ V) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const double l = rw.len[i];
+    const double wminus = 0.5 * l / rw.am[i];
+    const double wplus = 0.5 * l / rw.ap[i];
+    double2 v = make_double2(0.0, 0.0);
+    for (int side = 0; side < 2; side++) {
+        const int64_t t = side == 0 ? rw.itm[i] : rw.itp[i];
+        const double* pf = side == 0 ? rw.vm + 3 * i : rw.vp + 3 * i;
+        const double wside = side == 0 ? wminus : wplus;
+        for (int q = 0; q < nq; q++) {
+            const double* x = qp + 4 * (t * nq + q);
+            double2 E[3];
+            pw_field(pw, k, x, E);
+            double2 dotv = make_double2(0.0, 0.0);
+            for (int a = 0; a < 3; a++) dotv = cadd(dotv, cscale(E[a], x[a] - pf[a]));
+            double2 term = cscale(dotv, wside * x[3]);
+            v = side == 0 ? csub(v, term) : cadd(v, term);
+        }
+    }
+    // v / (0 - j omega mu0) = (-v.im, v.re) / (omega mu0)
+    const double a = omega * FRICO_MU0;
+    V[i] = cadd(V[i], make_double2(-v.y / a, v.x / a));
+}
+
+// Current lumping: per triangle, contributions of its (<= 3) RWGs in
+// increasing matrix index, as run_context accumulates them.
+__global__ void k_lump(int64_t nt, const TriGeo* __restrict__ geo, const int32_t* __restrict__ tri_bf,
+                       RwgDev rw, const double2* __restrict__ I, double2* __restrict__ AJ,
+                       double2* __restrict__ AdivJ, double2* __restrict__ J) {
+    int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (t >= nt) return;
+    const double* bar = geo[t].c;
+    const double A = geo[t].area;
+    double2 aj[3], jj[3], adj = make_double2(0, 0);
+    for (int a = 0; a < 3; a++) aj[a] = jj[a] = make_double2(0, 0);
+    for (int s = 0; s < 3; s++) {
+        int32_t e = tri_bf[3 * t + s];
+        if (e == 0) continue;
+        const int64_t i = (e < 0 ? -e : e) - 1;
+        const bool minus = e < 0;
+        const double l = rw.len[i];
+        const double area = minus ? rw.am[i] : rw.ap[i];
+        const double* pf = minus ? rw.vm + 3 * i : rw.vp + 3 * i;
+        const double2 Ie = I[i];
+        for (int a = 0; a < 3; a++) {
+            double f = minus ? (-l * (bar[a] - pf[a])) / (2.0 * area) : (l * (bar[a] - pf[a])) / (2.0 * area);
+            double2 Jv = cscale(Ie, f);
+            aj[a] = cadd(aj[a], cscale(Jv, A));
+            jj[a] = cadd(jj[a], Jv);
+        }
+        double div = minus ? -l / area : l / area;
+        adj = cadd(adj, cscale(Ie, A * div));
+    }
+    for (int a = 0; a < 3; a++) {
+        AJ[3 * t + a] = aj[a];
+        J[3 * t + a] = jj[a];
+    }
+    AdivJ[t] = adj;
+}
+
+static const int kFP = 128;   // points per CTA
+static const int kFT = 128;   // triangles staged per shared-memory round
+
+// Partial E/H sums for a block of points over one chunk of triangles.
+// part[(chunk * npts + p) * 6 + {Ex,Ey,Ez,Hx,Hy,Hz}]
+__global__ void __launch_bounds__(kFP) k_fields_part(int64_t npts, const double* __restrict__ P, int64_t nt,
+                                                    int64_t tri_per_chunk, const TriGeo* __restrict__ geo,
+                                                    const double2* __restrict__ AJ,
+                                                    const double2* __restrict__ AdivJ, double k, double omega,
+                                                    int hphase_physical, double2* __restrict__ part) {
+    __shared__ double sb[kFT][3];
+    __shared__ double2 sj[kFT][4];
+    const int64_t p = blockIdx.x * int64_t(kFP) + threadIdx.x;
+    const int64_t t0 = blockIdx.y * tri_per_chunk;
+    const int64_t t1 = min(nt, t0 + tri_per_chunk);
+    double px = 0, py = 0, pz = 0;
+    if (p < npts) { px = P[3 * p]; py = P[3 * p + 1]; pz = P[3 * p + 2]; }
+    double2 E[3], H[3];
+    for (int a = 0; a < 3; a++) E[a] = H[a] = make_double2(0, 0);
+    const double2 mjwmu = make_double2(-0.0 * FRICO_MU0, -omega * FRICO_MU0);  // (-j omega) * MU0
+    for (int64_t tb = t0; tb < t1; tb += kFT) {
+        const int cnt = int(min(int64_t(kFT), t1 - tb));
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const double* c = geo[tb + q].c;
+            sb[q][0] = c[0]; sb[q][1] = c[1]; sb[q][2] = c[2];
+            sj[q][0] = AJ[3 * (tb + q)];
+            sj[q][1] = AJ[3 * (tb + q) + 1];
+            sj[q][2] = AJ[3 * (tb + q) + 2];
+            sj[q][3] = AdivJ[tb + q];
+        }
+        __syncthreads();
+        if (p < npts)
+            for (int q = 0; q < cnt; q++) {
+                const double vx = px - sb[q][0], vy = py - sb[q][1], vz = pz - sb[q][2];
+                const double R = sqrt(vx * vx + vy * vy + vz * vz);
+                const double _4piR = 4 * M_PI * R;
+                const double _4piR3 = _4piR * R * R;
+                const double kR = k * R;
+                double s, c;
+                sincos(kR, &s, &c);
+                const double2 g = make_double2(c / _4piR, -s / _4piR);
+                const double2 J0 = sj[q][0], J1 = sj[q][1], J2 = sj[q][2];
+                const double2 t = cmul(sj[q][3], make_double2(1.0, kR));  // divJ*(1+jkR)
+                const double kR2 = kR * kR;
+                const double vr[3] = {vx, vy, vz};
+                const double2 Jv[3] = {J0, J1, J2};
+                for (int a = 0; a < 3; a++) {
+                    double2 tv = cscale(t, vr[a]);
+                    double2 d = csub(Jv[a], make_double2(tv.x / kR2, tv.y / kR2));
+                    E[a] = cadd(E[a], cmul(cmul(mjwmu, d), g));
+                }
+                // gradg = -((1+jkR)/_4piR3) * exp(+-jkR)
+                const double2 ph = hphase_physical ? make_double2(c, -s) : make_double2(c, s);
+                const double2 gg = cmul(make_double2(-(1.0 / _4piR3), -(kR / _4piR3)), ph);
+                const double2 rc[3] = {csub(cscale(J2, vy), cscale(J1, vz)), csub(cscale(J0, vz), cscale(J2, vx)),
+                                       csub(cscale(J1, vx), cscale(J0, vy))};
+                for (int a = 0; a < 3; a++) H[a] = cadd(H[a], cmul(rc[a], gg));
+            }
+    }
+    if (p < npts) {
+        double2* o = part + (blockIdx.y * npts + p) * 6;
+        for (int a = 0; a < 3; a++) { o[a] = E[a]; o[3 + a] = H[a]; }
+    }
+}
+
+__global__ void k_fields_reduce(int64_t npts, int nchunks, const double2* __restrict__ part,
+                                double2* __restrict__ out) {
+    int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (idx >= npts * 6) return;
+    double2 acc = make_double2(0, 0);
+    for (int c = 0; c < nchunks; c++) acc = cadd(acc, part[int64_t(c) * npts * 6 + idx]);
+    out[idx] = acc;
+}
+
+// ------------------------------------------------------------------ host side
+static RwgDev rwg_of(frico_gpu_ctx* ctx) {
+    RwgDev r;
+    r.itm = (int32_t*)ctx->rwg_itm.p;
+    r.itp = (int32_t*)ctx->rwg_itp.p;
+    r.len = (double*)ctx->rwg_len.p;
+    r.am = (double*)ctx->rwg_am.p;
+    r.ap = (double*)ctx->rwg_ap.p;
+    r.vm = (double*)ctx->rwg_vm.p;
+    r.vp = (double*)ctx->rwg_vp.p;
+    r.itf = (int32_t*)ctx->rwg_itf.p;
+    return r;
+}
+
+int rhs_delta_gap(frico_gpu_ctx* ctx, double freq, int col, int n_itf, const int32_t* tags, double2 V0,
+                  const double* signs) {
+    int rc;
+    const int64_t n = ctx->n;
+    const double omega = 2.0 * M_PI * freq;
+    // tags and signs go through one small device buffer
+    size_t bytes = sizeof(int32_t) * std::max(1, n_itf) + 16 + (signs ? sizeof(double) * n : 0);
+    DevBuf& tmp = ctx->fld_pts;
+    if ((rc = ensure(ctx, tmp, bytes))) return rc;
+    int32_t* dtags = (int32_t*)tmp.p;
+    double* dsigns = signs ? (double*)((char*)tmp.p + ((sizeof(int32_t) * std::max(1, n_itf) + 15) & ~size_t(15))) : nullptr;
+    if (n_itf > 0 && (rc = cuda_check(ctx, cudaMemcpyAsync(dtags, tags, sizeof(int32_t) * n_itf,
+                                                          cudaMemcpyHostToDevice, ctx->stream), "tags")))
+        return rc;
+    if (signs && (rc = cuda_check(ctx, cudaMemcpyAsync(dsigns, signs, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                                       ctx->stream), "signs")))
+        return rc;
+    k_rhs_delta_gap<<<unsigned((n + 255) / 256), 256, 0, ctx->stream>>>(
+        n, (const int32_t*)ctx->rwg_itf.p, (const double*)ctx->rwg_len.p, omega, dtags, n_itf, V0, dsigns,
+        (double2*)ctx->rhs.p + int64_t(col) * n);
+    count_launch(ctx);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "k_rhs_delta_gap"))) return rc;
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "rhs sync");
+}
+
+int rhs_plane_wave(frico_gpu_ctx* ctx, double freq, int col, double theta, double phi, double2 Eth, double2 Eph) {
+    int rc;
+    if (ctx->geo_degree != ctx->opt.degree)
+        if ((rc = build_quadrature(ctx))) return rc;
+    const int64_t n = ctx->n;
+    const double omega = 2.0 * M_PI * freq;
+    const double k = omega * std::sqrt(FRICO_MU0 * FRICO_EPS0);
+    PlaneWave pw;
+    pw.dir[0] = std::sin(theta) * std::cos(phi);
+    pw.dir[1] = std::sin(theta) * std::sin(phi);
+    pw.dir[2] = std::cos(theta);
+    pw.th[0] = std::cos(theta) * std::cos(phi);
+    pw.th[1] = std::cos(theta) * std::sin(phi);
+    pw.th[2] = -std::sin(theta);
+    pw.ph[0] = -std::sin(phi);
+    pw.ph[1] = std::cos(phi);
+    pw.ph[2] = 0.0;
+    pw.Eth = Eth;
+    pw.Eph = Eph;
+    k_rhs_plane_wave<<<unsigned((n + 127) / 128), 128, 0, ctx->stream>>>(
+        n, rwg_of(ctx), (const double*)ctx->qp.p, ctx->nq, k, omega, pw, (double2*)ctx->rhs.p + int64_t(col) * n);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_rhs_plane_wave");
+}
+
+int lump_currents(frico_gpu_ctx* ctx, int col) {
+    int rc;
+    const int64_t nt = ctx->nt, n = ctx->n;
+    if ((rc = ensure(ctx, ctx->tri_aj, sizeof(double2) * 3 * nt))) return rc;
+    if ((rc = ensure(ctx, ctx->tri_adivj, sizeof(double2) * nt))) return rc;
+    if ((rc = ensure(ctx, ctx->tri_j, sizeof(double2) * 3 * nt))) return rc;
+    k_lump<<<unsigned((nt + 127) / 128), 128, 0, ctx->stream>>>(
+        nt, (const TriGeo*)ctx->trigeo.p, (const int32_t*)ctx->tri_bf.p, rwg_of(ctx),
+        (const double2*)ctx->sol.p + int64_t(col) * n, (double2*)ctx->tri_aj.p, (double2*)ctx->tri_adivj.p,
+        (double2*)ctx->tri_j.p);
+    count_launch(ctx);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "k_lump"))) return rc;
+    ctx->lumped_col = col;
+    return FRICO_GPU_OK;
+}
+
+int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_host, double2* E_host,
+                    double2* H_host) {
+    int rc;
+    if (ctx->lumped_col != col)
+        if ((rc = lump_currents(ctx, col))) return rc;
+    const int64_t nt = ctx->nt;
+    const double omega = 2.0 * M_PI * ctx->freq;
+    const double k = omega * std::sqrt(FRICO_MU0 * FRICO_EPS0);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t pblocks = (npts + kFP - 1) / kFP;
+    // Enough (point block x triangle chunk) CTAs for ~8 per SM, chunks of >= 64 triangles.
+    int64_t nchunks = std::max<int64_t>(1, (int64_t(8) * sms + pblocks - 1) / pblocks);
+    nchunks = std::min<int64_t>(nchunks, std::max<int64_t>(1, nt / 64));
+    const int64_t tpc = (nt + nchunks - 1) / nchunks;
+    nchunks = (nt + tpc - 1) / tpc;
+    if ((rc = ensure(ctx, ctx->fld_part, sizeof(double2) * 6 * npts * nchunks))) return rc;
+    if ((rc = ensure(ctx, ctx->fld_out, sizeof(double2) * 6 * npts))) return rc;
+    DevBuf& pts = ctx->fld_pts;
+    if ((rc = ensure(ctx, pts, sizeof(double) * 3 * npts))) return rc;
+    if ((rc = cuda_check(ctx, cudaMemcpyAsync(pts.p, P_host, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice,
+                                              ctx->stream), "points")))
+        return rc;
+    k_fields_part<<<dim3(unsigned(pblocks), unsigned(nchunks)), kFP, 0, ctx->stream>>>(
+        npts, (const double*)pts.p, nt, tpc, (const TriGeo*)ctx->trigeo.p, (const double2*)ctx->tri_aj.p,
+        (const double2*)ctx->tri_adivj.p, k, omega, ctx->opt.h_phase_mode == FRICO_HPHASE_PHYSICAL,
+        (double2*)ctx->fld_part.p);
+    k_fields_reduce<<<unsigned((npts * 6 + 255) / 256), 256, 0, ctx->stream>>>(
+        npts, int(nchunks), (const double2*)ctx->fld_part.p, (double2*)ctx->fld_out.p);
+    count_launch(ctx, 2);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "fields kernels"))) return rc;
+    if (E_host || H_host) {
+        std::vector<double2> h(6 * npts);
+        if ((rc = cuda_check(ctx, cudaMemcpyAsync(h.data(), ctx->fld_out.p, sizeof(double2) * 6 * npts,
+                                                  cudaMemcpyDeviceToHost, ctx->stream), "fields out")))
+            return rc;
+        if ((rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "fields sync"))) return rc;
+        for (int64_t p = 0; p < npts; p++)
+            for (int a = 0; a < 3; a++) {
+                if (E_host) E_host[3 * p + a] = h[6 * p + a];
+                if (H_host) H_host[3 * p + a] = h[6 * p + 3 + a];
+            }
+    }
+    return FRICO_GPU_OK;
+}
+
+}  // namespace frico

@@ -1,0 +1,511 @@
+// EFIE impedance-matrix fill (FRICO compute_matrix / compute_matrix_approx).
+//
+// Reference: src/emw_solver.cpp:45-142 (quadrature fill) and :144-220 (MOM3D
+// centroid fill). FRICO loops over RWG pairs (i, j) and, for each of the four
+// triangle blocks (T_i-/+, T_j-/+), evaluates the Green function at every pair
+// of quadrature points. The same Green value is therefore recomputed for every
+// RWG pair that shares a triangle pair (9x at degree 1).
+//
+// GB300 layout of the same arithmetic:
+//   phase 1  gtab: one Green evaluation per ordered triangle pair (a, b)
+//            (degree 1: g = exp(-jkR)/R; degree >= 2: 8 weighted moments of g),
+//            stored row-major [a][b] in HBM (Nt^2 * 16 B at degree 1).
+//   phase 1' split moments: for every RWG i and side s the two blocks whose
+//            source triangle is T_i- or T_i+ use integrate_subtri on the
+//            source (src/emw_solver.cpp:67-78); their 8 moments are computed
+//            once per (i, s, source) with FP64 throughout.
+//   phase 2  assembly: one thread per Z entry (row j, column i); a CTA owns a
+//            run of rows of one column, so stores are coalesced and the
+//            column's RWG data is a broadcast. Each block is rebuilt from the
+//            table with FRICO's own expression
+//               entry += prodl * w * (v - 1/k^2) * g      (:81-137)
+//            or, for split / higher-degree blocks, from the moments
+//               F = 1/4 (Mpq - u.Mp - v.Mq + (v.u) M0) - M0/k^2
+//            which is the same double sum expanded about the two centroids.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "dunavant_rules.h"
+
+namespace frico {
+
+__constant__ double c_orbits[160][5];
+__constant__ int c_first[21];
+
+// ------------------------------------------------------------------ geometry
+__device__ __forceinline__ double dnorm3(double x, double y, double z) { return sqrt(x * x + y * y + z * z); }
+
+// area_triangle_kahan, src/quadratures.cpp:41-57
+__device__ double kahan_area(const double* p0, const double* p1, const double* p2) {
+    double l10 = dnorm3(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]);
+    double l20 = dnorm3(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]);
+    double l21 = dnorm3(p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]);
+    // sort ascending
+    double s0 = l10, s1 = l20, s2 = l21, t;
+    if (s1 < s0) { t = s0; s0 = s1; s1 = t; }
+    if (s2 < s1) { t = s1; s1 = s2; s2 = t; }
+    if (s1 < s0) { t = s0; s0 = s1; s1 = t; }
+    double a = s2, b = s1, c = s0;
+    return 0.25 * sqrt((a + (b + c)) * (c - (a - b)) * (c + (a - b)) * (a + (b - c)));
+}
+
+// dunavant(degree, p0, p1, p2), src/quadratures.cpp:321-372: writes the points
+// in FRICO's permutation order; returns the number written. out[4*k] = x,y,z,w.
+__device__ int dunavant_points(int degree, const double* p0, const double* p1, const double* p2,
+                               double* out) {
+    int rule = degree == 0 ? 0 : degree - 1;
+    double area = kahan_area(p0, p1, p2);
+    int k = 0;
+    for (int e = c_first[rule]; e < c_first[rule + 1]; e++) {
+        int perms = int(c_orbits[e][0]);
+        double l0 = c_orbits[e][1], l1 = c_orbits[e][2], l2 = c_orbits[e][3], w = c_orbits[e][4] * area;
+        double L[6][3];
+        int np;
+        if (perms == 1) {
+            L[0][0] = l0; L[0][1] = l1; L[0][2] = l2; np = 1;
+        } else if (perms == 3) {
+            L[0][0] = l0; L[0][1] = l1; L[0][2] = l2;
+            L[1][0] = l1; L[1][1] = l2; L[1][2] = l0;
+            L[2][0] = l1; L[2][1] = l0; L[2][2] = l2; np = 3;
+        } else {
+            L[0][0] = l0; L[0][1] = l1; L[0][2] = l2;
+            L[1][0] = l0; L[1][1] = l2; L[1][2] = l1;
+            L[2][0] = l1; L[2][1] = l0; L[2][2] = l2;
+            L[3][0] = l1; L[3][1] = l2; L[3][2] = l0;
+            L[4][0] = l2; L[4][1] = l0; L[4][2] = l1;
+            L[5][0] = l2; L[5][1] = l1; L[5][2] = l0; np = 6;
+        }
+        for (int q = 0; q < np; q++) {
+            for (int d = 0; d < 3; d++)
+                out[4 * k + d] = __dadd_rn(__dadd_rn(__dmul_rn(p0[d], L[q][0]), __dmul_rn(p1[d], L[q][1])),
+                                           __dmul_rn(p2[d], L[q][2]));
+            out[4 * k + 3] = w;
+            k++;
+        }
+    }
+    return k;
+}
+
+// Per triangle: geometry, integrate() points and integrate_subtri() points
+// (src/quadratures.cpp:2678-2702): sub-triangles (v0,v1,c), (v1,v2,c), (v2,v0,c).
+__global__ void k_build_quadrature(int64_t nt, const double* __restrict__ xyz,
+                                   const int64_t* __restrict__ tri, int degree, int nq,
+                                   TriGeo* __restrict__ geo, double* __restrict__ qp,
+                                   double* __restrict__ qps) {
+    int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (t >= nt) return;
+    double p[3][3];
+    for (int k = 0; k < 3; k++)
+        for (int d = 0; d < 3; d++) p[k][d] = xyz[3 * tri[3 * t + k] + d];
+    TriGeo g;
+    for (int k = 0; k < 3; k++)
+        for (int d = 0; d < 3; d++) g.v[3 * k + d] = p[k][d];
+    // barycenter: (p0 + p1 + p2) / 3.0, src/geom_mesh.cpp:64-69
+    for (int d = 0; d < 3; d++) g.c[d] = __ddiv_rn(__dadd_rn(__dadd_rn(p[0][d], p[1][d]), p[2][d]), 3.0);
+    double e0[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+    double e1[3] = {p[2][0] - p[1][0], p[2][1] - p[1][1], p[2][2] - p[1][2]};
+    double cx = e0[1] * e1[2] - e0[2] * e1[1], cy = e0[2] * e1[0] - e0[0] * e1[2],
+           cz = e0[0] * e1[1] - e0[1] * e1[0];
+    g.area = 0.5 * dnorm3(cx, cy, cz);
+    g.area_kahan = kahan_area(p[0], p[1], p[2]);
+    g.pad[0] = g.pad[1] = 0.0;
+    geo[t] = g;
+    dunavant_points(degree, p[0], p[1], p[2], qp + 4 * nq * t);
+    double* o = qps + 12 * nq * t;
+    o += 4 * dunavant_points(degree, p[0], p[1], g.c, o);
+    o += 4 * dunavant_points(degree, p[1], p[2], g.c, o);
+    dunavant_points(degree, p[2], p[0], g.c, o);
+}
+
+// Per-RWG data used by the assembly. `a_m`/`a_p` depend on the fill mode:
+//   mode 0 (degree 1): rho at the single quadrature point, q - p_free
+//   mode 2 (MOM3D):    rho at the barycentre, c - p_free
+// `v_m`/`v_p` = p_free - centroid, the offsets the moment expansion needs.
+struct BasisAsm {
+    int32_t itm, itp;
+    double len, am, ap;
+    double a_m[3], a_p[3];
+    double v_m[3], v_p[3];
+    double w_m, w_p;
+};
+
+__global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo,
+                            const double* __restrict__ qp, int nq, int mode,
+                            BasisAsm* __restrict__ out) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    BasisAsm b;
+    b.itm = rw.itm[i];
+    b.itp = rw.itp[i];
+    b.len = rw.len[i];
+    b.am = rw.am[i];
+    b.ap = rw.ap[i];
+    const double* qm = qp + 4 * nq * int64_t(b.itm);
+    const double* qpp = qp + 4 * nq * int64_t(b.itp);
+    for (int d = 0; d < 3; d++) {
+        double vm = rw.vm[3 * i + d], vp = rw.vp[3 * i + d];
+        if (mode == 2) {
+            b.a_m[d] = geo[b.itm].c[d] - vm;
+            b.a_p[d] = geo[b.itp].c[d] - vp;
+        } else {
+            b.a_m[d] = qm[d] - vm;
+            b.a_p[d] = qpp[d] - vp;
+        }
+        b.v_m[d] = vm - geo[b.itm].c[d];
+        b.v_p[d] = vp - geo[b.itp].c[d];
+    }
+    b.w_m = qm[3];
+    b.w_p = qpp[3];
+    out[i] = b;
+}
+
+// ------------------------------------------------------------------ phase 1
+struct __align__(32) QPoint { double x, y, z, w; };
+
+// g(a, b) = exp(-j k R) / R between the single degree-1 points of a and b.
+__global__ void k_gtab_deg1(int64_t nt, const QPoint* __restrict__ qp, double k,
+                            double2* __restrict__ G) {
+    int64_t b = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    int64_t a = blockIdx.y;
+    if (b >= nt) return;
+    QPoint p = qp[a], q = qp[b];
+    double2 g = make_double2(0.0, 0.0);
+    if (a != b) {
+        double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        double R = sqrt(dx * dx + dy * dy + dz * dz);
+        double s, c;
+        sincos(k * R, &s, &c);
+        g = make_double2(c / R, -s / R);
+    }
+    G[a * nt + b] = g;
+}
+
+// MOM3D centroid Green function with the analytic self term,
+// src/emw_solver.cpp:181-214.
+__global__ void k_gtab_approx(int64_t nt, const TriGeo* __restrict__ geo, double k,
+                              double2* __restrict__ G) {
+    int64_t b = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    int64_t a = blockIdx.y;
+    if (b >= nt) return;
+    const double* ca = geo[a].c;
+    const double* cb = geo[b].c;
+    double2 g;
+    if (a != b) {
+        double dx = ca[0] - cb[0], dy = ca[1] - cb[1], dz = ca[2] - cb[2];
+        double R = sqrt(dx * dx + dy * dy + dz * dz);
+        double s, c;
+        sincos(k * R, &s, &c);
+        double den = 4.0 * M_PI * R;
+        g = make_double2(c / den, -s / den);
+    } else {
+        double sqrt_4pi = sqrt(4 * M_PI);
+        double sa = sqrt(geo[a].area);
+        // 0.25*(sqrt_4pi/sqrt_A - jk) * M_1_PI
+        g = make_double2(0.25 * (sqrt_4pi / sa) * M_1_PI, 0.25 * (-k) * M_1_PI);
+    }
+    G[a * nt + b] = g;
+}
+
+// Moments of g over point sets P (test, about ca) and Q (source, about cb):
+// m[0] = sum w w g, m[1..3] = sum w w g (p-ca), m[4..6] = sum w w g (q-cb),
+// m[7] = sum w w g (p-ca).(q-cb).
+__device__ void moments(const double* P, int np, const double* ca, const double* Q, int nq_,
+                        const double* cb, double k, double2* m) {
+    for (int c = 0; c < 8; c++) m[c] = make_double2(0.0, 0.0);
+    for (int ip = 0; ip < np; ip++) {
+        const double* p = P + 4 * ip;
+        double pl[3] = {p[0] - ca[0], p[1] - ca[1], p[2] - ca[2]};
+        for (int iq = 0; iq < nq_; iq++) {
+            const double* q = Q + 4 * iq;
+            double dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
+            double R = sqrt(dx * dx + dy * dy + dz * dz);
+            double s, c;
+            sincos(k * R, &s, &c);
+            double ww = p[3] * q[3];
+            double2 g = make_double2(ww * c / R, -ww * s / R);
+            double ql[3] = {q[0] - cb[0], q[1] - cb[1], q[2] - cb[2]};
+            double pq = pl[0] * ql[0] + pl[1] * ql[1] + pl[2] * ql[2];
+            m[0] = cadd(m[0], g);
+            for (int d = 0; d < 3; d++) {
+                m[1 + d] = cadd(m[1 + d], cscale(g, pl[d]));
+                m[4 + d] = cadd(m[4 + d], cscale(g, ql[d]));
+            }
+            m[7] = cadd(m[7], cscale(g, pq));
+        }
+    }
+}
+
+// Unsplit moments for every ordered triangle pair, degree >= 2. Planes of
+// nt*nt entries: M[c*nt*nt + a*nt + b].
+__global__ void k_gtab_moments(int64_t nt, const TriGeo* __restrict__ geo,
+                               const double* __restrict__ qp, int nq, double k,
+                               double2* __restrict__ M) {
+    int64_t b = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    int64_t a = blockIdx.y;
+    if (b >= nt) return;
+    double2 m[8];
+    if (a != b) {
+        moments(qp + 4 * nq * a, nq, geo[a].c, qp + 4 * nq * b, nq, geo[b].c, k, m);
+    } else {
+        for (int c = 0; c < 8; c++) m[c] = make_double2(0.0, 0.0);
+    }
+    int64_t plane = nt * nt;
+    for (int c = 0; c < 8; c++) M[c * plane + a * nt + b] = m[c];
+}
+
+// Split blocks: for RWG i, test side s (T_is, unsplit points) and source
+// triangle T_it (integrate_subtri points). S[(i*4 + 2*s + t)*8 + c].
+__global__ void k_split_moments(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo,
+                                const double* __restrict__ qp, const double* __restrict__ qps,
+                                int nq, double k, double2* __restrict__ S) {
+    int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (idx >= 4 * n) return;
+    int64_t i = idx >> 2;
+    int s = (idx >> 1) & 1, t = idx & 1;
+    int64_t ta = s == 0 ? rw.itm[i] : rw.itp[i];
+    int64_t tb = t == 0 ? rw.itm[i] : rw.itp[i];
+    double2 m[8];
+    moments(qp + 4 * nq * ta, nq, geo[ta].c, qps + 12 * nq * tb, 3 * nq, geo[tb].c, k, m);
+    for (int c = 0; c < 8; c++) S[idx * 8 + c] = m[c];
+}
+
+// ------------------------------------------------------------------ phase 2
+struct AsmArgs {
+    int64_t n, nt, ldz;
+    double inv_ksq;
+    const BasisAsm* bas;
+    const double2* G;    // mode 0/2: [nt*nt]; mode 1: 8 planes
+    const double2* S;    // split moments [n*4*8]
+    double2* Z64;        // may be null
+    float2* Z32;         // may be null
+};
+
+// F = 1/4 (Mpq - u.Mp - v.Mq + (v.u) M0) - M0 * inv_ksq
+__device__ __forceinline__ double2 moment_block(const double2* m, int64_t stride, const double* v,
+                                                const double* u, double inv_ksq) {
+    double2 m0 = m[0];
+    double2 acc = m[7 * stride];
+    for (int d = 0; d < 3; d++) {
+        acc = csub(acc, cscale(m[(1 + d) * stride], u[d]));
+        acc = csub(acc, cscale(m[(4 + d) * stride], v[d]));
+    }
+    double vu = v[0] * u[0] + v[1] * u[1] + v[2] * u[2];
+    acc = cadd(acc, cscale(m0, vu));
+    return csub(cscale(acc, 0.25), cscale(m0, inv_ksq));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_assemble(AsmArgs A) {
+    int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    int64_t i = blockIdx.y;
+    if (j >= A.n) return;
+    const BasisAsm bi = A.bas[i];
+    const BasisAsm bj = A.bas[j];
+    double2 entry = make_double2(0.0, 0.0);
+    const double prodl = 0.25 * bi.len * bj.len * M_1_PI;
+    const double lilj = bi.len * bj.len;
+#pragma unroll
+    for (int blk = 0; blk < 4; blk++) {
+        const int s = blk >> 1, t = blk & 1;  // order --, -+, +-, ++
+        const int32_t ta = s ? bi.itp : bi.itm;
+        const int32_t tb = t ? bj.itp : bj.itm;
+        const double ai = s ? bi.ap : bi.am;
+        const double aj = t ? bj.ap : bj.am;
+        const double* vi = s ? bi.a_p : bi.a_m;
+        const double* vj = t ? bj.a_p : bj.a_m;
+        const double* oi = s ? bi.v_p : bi.v_m;
+        const double* oj = t ? bj.v_p : bj.v_m;
+        double2 c;
+        if (MODE == 2) {
+            // src/emw_solver.cpp:181-215
+            double2 g = A.G[int64_t(ta) * A.nt + tb];
+            double rho = vi[0] * vj[0] + vi[1] * vj[1] + vi[2] * vj[2];
+            double2 d = csub(cscale(g, 0.25 * rho), cscale(g, A.inv_ksq));
+            c = cscale(d, lilj);
+        } else {
+            const double inv_AA = 1. / (ai * aj);
+            int split = (tb == bi.itm) ? 0 : (tb == bi.itp) ? 1 : -1;
+            if (split >= 0) {
+                const double2* m = A.S + (i * 4 + 2 * s + split) * 8;
+                double2 F = moment_block(m, 1, oi, oj, A.inv_ksq);
+                c = cscale(F, prodl * inv_AA);
+            } else if (MODE == 0) {
+                // src/emw_solver.cpp:85-94
+                double v = 0.25 * (vi[0] * vj[0] + vi[1] * vj[1] + vi[2] * vj[2]);
+                double w = (s ? bi.w_p : bi.w_m) * (t ? bj.w_p : bj.w_m) * inv_AA;
+                double2 g = A.G[int64_t(ta) * A.nt + tb];
+                c = cscale(g, prodl * w * (v - A.inv_ksq));
+            } else {
+                int64_t plane = A.nt * A.nt;
+                double2 F = moment_block(A.G + int64_t(ta) * A.nt + tb, plane, oi, oj, A.inv_ksq);
+                c = cscale(F, prodl * inv_AA);
+            }
+        }
+        entry = (s == t) ? cadd(entry, c) : csub(entry, c);
+    }
+    int64_t o = i * A.ldz + j;
+    if (A.Z64) A.Z64[o] = entry;
+    if (A.Z32) A.Z32[o] = make_float2(float(entry.x), float(entry.y));
+}
+
+// (Z + Z^T) / 2, src/emw_solver.h:118-120. Tiles of 32x32 above the diagonal
+// and their mirror images are exchanged through shared memory.
+__global__ void k_symmetrize(int64_t n, int64_t ld, double2* Z) {
+    __shared__ double2 ta[32][33], tb[32][33];
+    int64_t bi = blockIdx.y, bj = blockIdx.x;
+    if (bj < bi) return;
+    int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    for (int r = ty; r < 32; r += 8) {
+        int64_t row = bi * 32 + r, col = bj * 32 + tx;   // tile A: rows of block bi, cols of bj
+        ta[r][tx] = (row < n && col < n) ? Z[col * ld + row] : make_double2(0, 0);
+        int64_t row2 = bj * 32 + r, col2 = bi * 32 + tx;  // tile B: mirror
+        tb[r][tx] = (row2 < n && col2 < n) ? Z[col2 * ld + row2] : make_double2(0, 0);
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        int64_t row = bi * 32 + r, col = bj * 32 + tx;
+        if (row < n && col < n) {
+            double2 a = ta[r][tx], b = tb[tx][r];
+            Z[col * ld + row] = make_double2((a.x + b.x) / 2.0, (a.y + b.y) / 2.0);
+        }
+        int64_t row2 = bj * 32 + r, col2 = bi * 32 + tx;
+        if (bi != bj && row2 < n && col2 < n) {
+            double2 a = tb[r][tx], b = ta[tx][r];
+            Z[col2 * ld + row2] = make_double2((a.x + b.x) / 2.0, (a.y + b.y) / 2.0);
+        }
+    }
+}
+
+__global__ void k_z64_to_z32(int64_t count, const double2* __restrict__ a, float2* __restrict__ b) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < count) b[i] = make_float2(float(a[i].x), float(a[i].y));
+}
+
+// ------------------------------------------------------------------ host side
+static bool g_tables_loaded = false;
+
+int build_quadrature(frico_gpu_ctx* ctx) {
+    int degree = ctx->opt.degree;
+    if (degree < 0 || degree > frico_tables::kDunavantMaxDegree)
+        return set_err(ctx, FRICO_GPU_EINVAL, "Dunavant quadrature: degree too high");
+    if (!g_tables_loaded) {
+        int rc = cuda_check(ctx, cudaMemcpyToSymbol(c_orbits, frico_tables::kDunavantOrbits,
+                                                    sizeof(frico_tables::kDunavantOrbits)),
+                            "copy Dunavant table");
+        if (rc) return rc;
+        rc = cuda_check(ctx, cudaMemcpyToSymbol(c_first, frico_tables::kDunavantFirst,
+                                                sizeof(frico_tables::kDunavantFirst)),
+                        "copy Dunavant offsets");
+        if (rc) return rc;
+        g_tables_loaded = true;
+    }
+    int rule = degree == 0 ? 0 : degree - 1;
+    int nq = frico_tables::kDunavantPoints[rule];
+    int64_t nt = ctx->nt;
+    int rc;
+    if ((rc = ensure(ctx, ctx->trigeo, sizeof(TriGeo) * nt))) return rc;
+    if ((rc = ensure(ctx, ctx->qp, sizeof(double) * 4 * nq * nt))) return rc;
+    if ((rc = ensure(ctx, ctx->qps, sizeof(double) * 12 * nq * nt))) return rc;
+    k_build_quadrature<<<unsigned((nt + 127) / 128), 128, 0, ctx->stream>>>(
+        nt, (const double*)ctx->xyz.p, (const int64_t*)ctx->tri.p, degree, nq, (TriGeo*)ctx->trigeo.p,
+        (double*)ctx->qp.p, (double*)ctx->qps.p);
+    count_launch(ctx);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "k_build_quadrature"))) return rc;
+    ctx->nq = nq;
+    ctx->geo_degree = degree;
+    return FRICO_GPU_OK;
+}
+
+static RwgDev rwg_dev(frico_gpu_ctx* ctx) {
+    RwgDev r;
+    r.itm = (int32_t*)ctx->rwg_itm.p;
+    r.itp = (int32_t*)ctx->rwg_itp.p;
+    r.len = (double*)ctx->rwg_len.p;
+    r.am = (double*)ctx->rwg_am.p;
+    r.ap = (double*)ctx->rwg_ap.p;
+    r.vm = (double*)ctx->rwg_vm.p;
+    r.vp = (double*)ctx->rwg_vp.p;
+    r.itf = (int32_t*)ctx->rwg_itf.p;
+    return r;
+}
+
+int fill_matrix(frico_gpu_ctx* ctx, double freq) {
+    int rc;
+    if (ctx->geo_degree != ctx->opt.degree)
+        if ((rc = build_quadrature(ctx))) return rc;
+    const int64_t n = ctx->n, nt = ctx->nt;
+    const int nq = ctx->nq;
+    const int mode = ctx->opt.approx ? 2 : (nq == 1 ? 0 : 1);
+    // src/emw_solver.cpp:51-54
+    const double omega = 2.0 * M_PI * freq;
+    const double k = omega * std::sqrt(FRICO_MU0 * FRICO_EPS0);
+    const double inv_ksq = 1. / (omega * omega * FRICO_MU0 * FRICO_EPS0);
+
+    if ((rc = ensure(ctx, ctx->basis_aux, sizeof(BasisAsm) * n))) return rc;
+    const size_t gbytes = sizeof(double2) * size_t(nt) * size_t(nt) * (mode == 1 ? 8 : 1);
+    if ((rc = ensure(ctx, ctx->gtab, gbytes))) return rc;
+    if (mode != 2 && (rc = ensure(ctx, ctx->smom, sizeof(double2) * 32 * n))) return rc;
+    if ((rc = ensure(ctx, ctx->z64, sizeof(double2) * size_t(n) * size_t(n)))) return rc;
+    const bool want32 = ctx->opt.precision == FRICO_PREC_MIXED && !ctx->opt.force_symmetry;
+    if (want32 && (rc = ensure(ctx, ctx->z32, sizeof(float2) * size_t(n) * size_t(n)))) return rc;
+
+    RwgDev rw = rwg_dev(ctx);
+    const TriGeo* geo = (const TriGeo*)ctx->trigeo.p;
+    const double* qp = (const double*)ctx->qp.p;
+    const double* qps = (const double*)ctx->qps.p;
+    cudaStream_t st = ctx->stream;
+    k_basis_aux<<<unsigned((n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, nq, mode,
+                                                           (BasisAsm*)ctx->basis_aux.p);
+    dim3 gt(unsigned((nt + 127) / 128), unsigned(nt));
+    double2* G = (double2*)ctx->gtab.p;
+    if (mode == 0) {
+        k_gtab_deg1<<<gt, 128, 0, st>>>(nt, (const QPoint*)qp, k, G);
+    } else if (mode == 1) {
+        k_gtab_moments<<<gt, 128, 0, st>>>(nt, geo, qp, nq, k, G);
+    } else {
+        k_gtab_approx<<<gt, 128, 0, st>>>(nt, geo, k, G);
+    }
+    if (mode != 2)
+        k_split_moments<<<unsigned((4 * n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, qps, nq, k,
+                                                                        (double2*)ctx->smom.p);
+    AsmArgs a;
+    a.n = n;
+    a.nt = nt;
+    a.ldz = n;
+    a.inv_ksq = inv_ksq;
+    a.bas = (const BasisAsm*)ctx->basis_aux.p;
+    a.G = G;
+    a.S = (const double2*)ctx->smom.p;
+    a.Z64 = (double2*)ctx->z64.p;
+    a.Z32 = want32 ? (float2*)ctx->z32.p : nullptr;
+    dim3 ga(unsigned((n + 255) / 256), unsigned(n));
+    if (mode == 0) k_assemble<0><<<ga, 256, 0, st>>>(a);
+    else if (mode == 1) k_assemble<1><<<ga, 256, 0, st>>>(a);
+    else k_assemble<2><<<ga, 256, 0, st>>>(a);
+    count_launch(ctx, mode != 2 ? 4 : 3);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "fill kernels"))) return rc;
+    if (ctx->opt.force_symmetry) {
+        if ((rc = symmetrize(ctx))) return rc;
+        if (ctx->opt.precision == FRICO_PREC_MIXED) {
+            if ((rc = ensure(ctx, ctx->z32, sizeof(float2) * size_t(n) * size_t(n)))) return rc;
+            int64_t cnt = n * n;
+            k_z64_to_z32<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, (const double2*)ctx->z64.p,
+                                                                   (float2*)ctx->z32.p);
+            if ((rc = cuda_check(ctx, cudaGetLastError(), "k_z64_to_z32"))) return rc;
+        }
+    }
+    // Algorithmic Green evaluations: ordered pairs x nq^2, plus the split blocks.
+    ctx->stats.green_evals = mode == 2 ? nt * nt : nt * (nt - 1) * int64_t(nq) * nq + 4 * n * int64_t(nq) * 3 * nq;
+    ctx->freq = freq;
+    return FRICO_GPU_OK;
+}
+
+int symmetrize(frico_gpu_ctx* ctx) {
+    int64_t n = ctx->n;
+    unsigned nb = unsigned((n + 31) / 32);
+    k_symmetrize<<<dim3(nb, nb), dim3(32, 8), 0, ctx->stream>>>(n, n, (double2*)ctx->z64.p);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_symmetrize");
+}
+
+}  // namespace frico

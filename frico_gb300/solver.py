@@ -1,0 +1,308 @@
+"""Host-side mirror of FRICO's solver interface over libfrico_gpu.
+
+FRICO's C++ surface (src/emw_solver.h:41-173, src/emw_postpro_common.h:33-37,
+src/emw_ana_antenna.h:31-52, src/emw_ana_bistatic_rcs.h:28-45) becomes:
+
+  Simulation(mesh, degree=1, approx_matrix=False, force_symmetry=False, Z0=50)
+                                            simulation + config
+  sim.compute_matrix(freq)                  compute_matrix / compute_matrix_approx
+  sim.update_rhs(freq, DeltaGap|PlaneWave)  update_rhs(delta_gap | plane_wave)
+  sim.solve()                               solve_general / solve_symmetric
+  sim.run_context(freq, source)             run_context (fill, rhs, solve, lumping)
+  sim.eval_fields(points)                   eval_fields(sim, ctx, point) over many points
+  sim.port_values(dgap)                     compute_port_values
+  sim.compute_gain(pwr, R, plane)           compute_gain
+  sim.bistatic_rcs(R)                       the 359-angle loop of postpro_context
+  do_sweep_antenna / do_sweep_bistatic      do_sweep(sim, antenna_analysis | bistatic_rcs_analysis)
+
+Every numeric stage runs in the CUDA library; errors come back as FricoError
+carrying FRICO_GPU_* codes (FRICO prints to stderr and returns false).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from ._abi import FricoError, ptr
+from .meshes import TriMesh
+
+
+@dataclass
+class DeltaGap:
+    """src/sources.h:78-83"""
+    interfaces: tuple
+    voltage: complex = 1.0
+    name: str = "feed"
+
+
+@dataclass
+class PlaneWave:
+    """src/sources.h:34-75 (theta, phi in radians)"""
+    theta: float
+    phi: float
+    Etheta: complex = 1.0
+    Ephi: complex = 1.0
+
+
+@dataclass
+class FunctionSpace:
+    rwg: np.ndarray               # RWG_DTYPE[n]
+    edge_vertices: np.ndarray     # (n, 2) int64
+    vertices: np.ndarray          # compacted (nv, 3)
+    triangles: np.ndarray         # (nt, 3) int64
+    tri_tags: np.ndarray          # (nt,)
+
+    @property
+    def n(self) -> int:
+        return int(self.rwg.shape[0])
+
+
+def _check(lib, code: int, ctx=None, what: str = ""):
+    if code != _abi.OK:
+        msg = lib.frico_gpu_last_error(ctx).decode() if ctx else what
+        raise FricoError(code, msg or what)
+
+
+def make_function_space(mesh: TriMesh, edge_length: str = "xy") -> FunctionSpace:
+    """load_from_gmsh connectivity + make_function_space (host C++ in the library)."""
+    lib = _abi.load()
+    mode = _abi.EDGE_LENGTH_XY if edge_length == "xy" else _abi.EDGE_LENGTH_TRUE
+    V = np.ascontiguousarray(mesh.vertices, np.float64)
+    T = np.ascontiguousarray(mesh.triangles, np.int64)
+    Cv = np.ascontiguousarray(mesh.curves, np.int64).reshape(-1, 2)
+    Ct = np.ascontiguousarray(mesh.curve_tags, np.int32)
+    nrwg = C.c_int64(0)
+    nvo = C.c_int64(0)
+    cap = 3 * mesh.nt // 2 + 3
+    rwg = np.zeros(cap, _abi.RWG_DTYPE)
+    ev = np.zeros((cap, 2), np.int64)
+    vout = np.zeros_like(V)
+    tout = np.zeros_like(T)
+    rc = lib.frico_gpu_make_function_space(mesh.nv, ptr(V), mesh.nt, ptr(T), Cv.shape[0], ptr(Cv), ptr(Ct), mode,
+                                           ptr(rwg), cap, C.byref(nrwg), ptr(ev), ptr(vout), C.byref(nvo), ptr(tout))
+    _check(lib, rc, what="make_function_space")
+    n = nrwg.value
+    return FunctionSpace(rwg[:n].copy(), ev[:n].copy(), vout[: nvo.value].copy(), tout, mesh.tri_tags.copy())
+
+
+def reorient_deltagap_edges(fs: FunctionSpace, interfaces, force: bool = False):
+    """Returns the sign vector (None when FRICO would leave delta_gap_signs empty)."""
+    lib = _abi.load()
+    tags = np.asarray(interfaces, np.int32)
+    signs = np.ones(fs.n)
+    applied = C.c_int32(0)
+    tt = np.ascontiguousarray(fs.tri_tags, np.int32)
+    rc = lib.frico_gpu_reorient_deltagap(fs.vertices.shape[0], ptr(fs.vertices), ptr(fs.triangles), ptr(tt), fs.n,
+                                         ptr(fs.rwg), ptr(fs.edge_vertices), len(tags), ptr(tags), int(force),
+                                         ptr(signs), C.byref(applied))
+    _check(lib, rc, what="reorient_deltagap_edges: feed edges missing or not connected")
+    return signs if applied.value else None
+
+
+class Simulation:
+    def __init__(self, mesh: TriMesh, degree: int = 1, approx_matrix: bool = False,
+                 force_symmetry: bool = False, precision: str = "fp64", Z0: float = 50.0,
+                 h_phase: str = "compat", edge_length: str = "xy", device: int = 0,
+                 max_refine_iters: int = 30, refine_tol: float = 1e-12, profile_kernels: bool = False):
+        self.lib = _abi.load()
+        self.mesh = mesh
+        self.fs = make_function_space(mesh, edge_length)
+        self.opt = _abi.Options(degree, int(approx_matrix), int(force_symmetry),
+                                _abi.PREC_MIXED if precision == "mixed" else _abi.PREC_FP64,
+                                _abi.HPHASE_PHYSICAL if h_phase == "physical" else _abi.HPHASE_COMPAT,
+                                max_refine_iters, refine_tol, Z0, int(profile_kernels), 0)
+        self.ctx = C.c_void_p()
+        rc = self.lib.frico_gpu_ctx_create(C.byref(self.ctx), device, C.byref(self.opt))
+        _check(self.lib, rc, what="frico_gpu_ctx_create (is a CUDA device visible?)")
+        fs = self.fs
+        self._call("frico_gpu_set_mesh", fs.vertices.shape[0], ptr(fs.vertices), fs.triangles.shape[0],
+                   ptr(fs.triangles), fs.n, ptr(fs.rwg))
+        self.freq = None
+        self.nrhs = 0
+        self.delta_gap_signs = None
+
+    # -- plumbing
+    def _call(self, name, *args):
+        rc = getattr(self.lib, name)(self.ctx, *args)
+        if rc != _abi.OK:
+            raise FricoError(rc, self.lib.frico_gpu_last_error(self.ctx).decode())
+        return rc
+
+    def close(self):
+        if self.ctx:
+            self.lib.frico_gpu_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n(self) -> int:
+        return self.fs.n
+
+    @property
+    def nt(self) -> int:
+        return int(self.fs.triangles.shape[0])
+
+    def set_options(self, **kw):
+        for k, v in kw.items():
+            if k == "precision":
+                v = _abi.PREC_MIXED if v == "mixed" else _abi.PREC_FP64
+            setattr(self.opt, k, int(v) if k != "refine_tol" and k != "Z0" else float(v))
+        self._call("frico_gpu_set_options", C.byref(self.opt))
+
+    # -- stages
+    def compute_matrix(self, freq: float, download: bool = False):
+        Z = np.empty((self.n, self.n), np.complex128, order="F") if download else None
+        self._call("frico_gpu_fill", float(freq), ptr(Z), self.n)
+        self.freq = float(freq)
+        return Z
+
+    def set_nrhs(self, nrhs: int):
+        self._call("frico_gpu_set_nrhs", int(nrhs))
+        self.nrhs = int(nrhs)
+
+    def update_rhs(self, freq: float, src, col: int = 0):
+        if self.nrhs <= col:
+            self.set_nrhs(col + 1)
+        if isinstance(src, DeltaGap):
+            tags = np.asarray(src.interfaces, np.int32)
+            v = complex(src.voltage)
+            signs = None if self.delta_gap_signs is None else np.ascontiguousarray(self.delta_gap_signs)
+            self._call("frico_gpu_rhs_delta_gap", float(freq), col, len(tags), ptr(tags), _abi.C128(v.real, v.imag),
+                       ptr(signs))
+        elif isinstance(src, PlaneWave):
+            a, b = complex(src.Etheta), complex(src.Ephi)
+            self._call("frico_gpu_rhs_plane_wave", float(freq), col, float(src.theta), float(src.phi),
+                       _abi.C128(a.real, a.imag), _abi.C128(b.real, b.imag))
+        else:
+            raise TypeError("source must be DeltaGap or PlaneWave")
+
+    def get_rhs(self) -> np.ndarray:
+        V = np.empty((self.n, self.nrhs), np.complex128, order="F")
+        self._call("frico_gpu_get_rhs", ptr(V), self.n)
+        return V
+
+    def set_rhs(self, V: np.ndarray):
+        V = np.asfortranarray(np.asarray(V, np.complex128).reshape(self.n, -1))
+        self._call("frico_gpu_set_rhs", V.shape[1], ptr(V), self.n)
+        self.nrhs = V.shape[1]
+
+    def solve(self, download: bool = True):
+        I = np.empty((self.n, self.nrhs), np.complex128, order="F") if download else None
+        info = C.c_int32(0)
+        self._call("frico_gpu_solve", ptr(I), self.n, C.byref(info))
+        return I
+
+    def get_factors(self):
+        LU = np.empty((self.n, self.n), np.complex128, order="F")
+        ipiv = np.empty(self.n, np.int32)
+        self._call("frico_gpu_get_factors", ptr(LU), self.n, ptr(ipiv))
+        return LU, ipiv
+
+    def lump_currents(self, col: int = 0):
+        AJ = np.empty((self.nt, 3), np.complex128)
+        AdivJ = np.empty(self.nt, np.complex128)
+        J = np.empty((self.nt, 3), np.complex128)
+        self._call("frico_gpu_lump_currents", col, ptr(AJ), ptr(AdivJ), ptr(J))
+        return AJ, AdivJ, J
+
+    def eval_fields(self, points: np.ndarray, col: int = 0):
+        Pt = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        E = np.empty((Pt.shape[0], 3), np.complex128)
+        H = np.empty((Pt.shape[0], 3), np.complex128)
+        self._call("frico_gpu_eval_fields", col, Pt.shape[0], ptr(Pt), ptr(E), ptr(H))
+        return E, H
+
+    def port_values(self, dg: DeltaGap, col: int = 0) -> dict:
+        tags = np.asarray(dg.interfaces, np.int32)
+        v = complex(dg.voltage)
+        pv = _abi.PortValues()
+        signs = None if self.delta_gap_signs is None else np.ascontiguousarray(self.delta_gap_signs)
+        self._call("frico_gpu_port_values", col, len(tags), ptr(tags), _abi.C128(v.real, v.imag), ptr(signs),
+                   C.byref(pv))
+        c = lambda z: complex(z.re, z.im)  # noqa: E731
+        return {"voltage": c(pv.voltage), "current": c(pv.current), "power": c(pv.power),
+                "impedance": c(pv.impedance), "gamma": c(pv.gamma), "swr": pv.swr}
+
+    def compute_gain(self, pwr: float, R: float, plane: int, col: int = 0) -> np.ndarray:
+        G = np.empty(360)
+        self._call("frico_gpu_gain", col, float(pwr), float(R), int(plane), ptr(G))
+        return G
+
+    def bistatic_rcs(self, R: float = 10.0, col: int = 0) -> np.ndarray:
+        out = np.empty((359, 4))
+        self._call("frico_gpu_bistatic_rcs", col, float(R), ptr(out))
+        return out
+
+    def rcs_points(self, R: float, theta, phi, col: int = 0) -> np.ndarray:
+        th = np.ascontiguousarray(theta, np.float64)
+        ph = np.ascontiguousarray(phi, np.float64)
+        out = np.empty((th.shape[0], 2))
+        self._call("frico_gpu_rcs_points", col, float(R), th.shape[0], ptr(th), ptr(ph), ptr(out))
+        return out
+
+    def stats(self) -> dict:
+        s = _abi.Stats()
+        self.lib.frico_gpu_last_stats(self.ctx, C.byref(s))
+        return {k: getattr(s, k) for k, _ in _abi.Stats._fields_}
+
+    # -- composite, src/emw_solver.h:92-167
+    def run_context(self, freq: float, src, download: bool = False):
+        self.compute_matrix(freq)
+        self.set_nrhs(1)
+        self.update_rhs(freq, src, 0)
+        I = self.solve(download=download)
+        self._call("frico_gpu_lump_currents", 0, None, None, None)
+        return I
+
+
+@dataclass
+class AntennaResult:
+    frequency: float
+    port: dict
+    gain_XY: np.ndarray
+    gain_YZ: np.ndarray
+    gain_XZ: np.ndarray
+
+
+def do_sweep_antenna(sim: Simulation, freqs, dgap: DeltaGap, rdiag_dist: float = 10.0,
+                     force_reorient: bool = False) -> list[AntennaResult]:
+    """do_sweep(sim, antenna_analysis), src/emw_ana_antenna.cpp:236-295 (no file output)."""
+    sim.delta_gap_signs = reorient_deltagap_edges(sim.fs, dgap.interfaces, force_reorient)
+    out = []
+    for f in freqs:
+        sim.run_context(f, dgap)
+        pv = sim.port_values(dgap)
+        pwr = pv["power"].real
+        gains = [sim.compute_gain(pwr, rdiag_dist, p) for p in (_abi.GAIN_XY, _abi.GAIN_YZ, _abi.GAIN_XZ)]
+        out.append(AntennaResult(float(f), pv, *gains))
+    return out
+
+
+@dataclass
+class BistaticAnalysis:
+    """src/emw_ana_bistatic_rcs.h:35-42 (angles in radians)"""
+    radar_R: float = 10.0
+    radar_theta: float = 0.0
+    radar_phi: float = 0.0
+    Etheta: float = 1.0
+    Ephi: float = 1.0
+    results: list = field(default_factory=list)
+
+
+def do_sweep_bistatic(sim: Simulation, freqs, ana: BistaticAnalysis) -> list[np.ndarray]:
+    """do_sweep(sim, bistatic_rcs_analysis), src/emw_ana_bistatic_rcs.cpp:120-151."""
+    pw = PlaneWave(ana.radar_theta, ana.radar_phi, ana.Etheta, ana.Ephi)
+    out = []
+    for f in freqs:
+        sim.run_context(f, pw)
+        out.append(sim.bistatic_rcs(ana.radar_R))
+    ana.results = out
+    return out

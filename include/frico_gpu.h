@@ -1,0 +1,218 @@
+/*
+ * frico_gpu.h -- C-ABI of the GB300 (sm_103a) Method-of-Moments hot path.
+ *
+ * The entry points replace FRICO's solver free functions one for one:
+ *
+ *   compute_matrix / compute_matrix_approx   src/emw_solver.h:85-86,  src/emw_solver.cpp:45-220
+ *   update_rhs(delta_gap | plane_wave)       src/emw_solver.h:87-88,  src/emw_solver.cpp:352-416
+ *   reorient_deltagap_edges                  src/emw_solver.h:90,     src/emw_solver.cpp:222-350
+ *   solve_general / solve_symmetric          src/lapack_wrappers.h:28-35
+ *   run_context (fill, rhs, solve, lumping)  src/emw_solver.h:92-167
+ *   eval_fields (point and point-set forms)  src/emw_postpro_common.h:33-34
+ *   compute_port_values, compute_gain        src/emw_ana_antenna.cpp:33-105
+ *   bistatic_RCS_unit_Ei + its 359-pt loop   src/emw_ana_bistatic_rcs.cpp:62-118
+ *   make_function_space + connectivity       src/rwg_basis.h:112, src/input_gmsh.cpp:216-322
+ *
+ * Conventions
+ *   - Complex numbers are two doubles {re, im} (layout of std::complex<double>);
+ *     matrices are column-major, entry (row j, col i) at j + i*ld, exactly as
+ *     FRICO's Eigen zdmatrix stores Z(jbf.matrix_index, ibf.matrix_index).
+ *   - Every function returns an int status (FRICO_GPU_OK or a negative code);
+ *     nothing aborts, nothing throws across the boundary.
+ *   - A context is used from one host thread at a time. Z, the LU factors,
+ *     right-hand sides and currents stay resident on the device; host output
+ *     pointers are optional (NULL = keep on device only).
+ *   - Host pointers may be pageable or pinned.
+ */
+#ifndef FRICO_GPU_H
+#define FRICO_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+#define FRICO_GPU_OK          0
+#define FRICO_GPU_EINVAL     -1   /* bad argument (FRICO: assert / invalid_argument) */
+#define FRICO_GPU_ESINGULAR  -2   /* exactly-zero pivot; *info holds the LAPACK info */
+#define FRICO_GPU_ETIMEOUT   -3   /* a bounded device-side wait gave up             */
+#define FRICO_GPU_ENOMEM     -4   /* device allocation failed                       */
+#define FRICO_GPU_ECUDA      -5   /* other CUDA runtime error                       */
+#define FRICO_GPU_ESTATE     -6   /* call out of order (e.g. solve before fill)     */
+#define FRICO_GPU_ENOCONV    -7   /* mixed-precision refinement did not converge    */
+#define FRICO_GPU_EMESH      -8   /* mesh connectivity error (lonely / multiple)    */
+
+/* ---- enums ---------------------------------------------------------- */
+#define FRICO_PREC_FP64       0   /* complex128 fill, LU and solve (the drop-in)     */
+#define FRICO_PREC_MIXED      1   /* complex64 LU + FP64 residual refinement        */
+
+#define FRICO_EDGE_LENGTH_XY   0  /* FRICO's measure(edge): hypot(dx, dy)           */
+#define FRICO_EDGE_LENGTH_TRUE 1  /* full 3-D length                                */
+
+#define FRICO_HPHASE_COMPAT    0  /* H kernel with exp(+jkR) as eval_fields has it  */
+#define FRICO_HPHASE_PHYSICAL  1  /* H kernel with exp(-jkR)                        */
+
+#define FRICO_GAIN_XY 0
+#define FRICO_GAIN_YZ 1
+#define FRICO_GAIN_XZ 2
+
+typedef struct frico_c128 { double re, im; } frico_c128;
+
+/* Mirrors frico::rwg_basis_function (src/rwg_basis.h:41-52). */
+typedef struct frico_rwg {
+    double  Aminus;          /* area of T-  (0.5 |e0 x e1|)                  */
+    double  Aplus;           /* area of T+                                   */
+    int64_t itminus;         /* index of T-                                  */
+    int64_t itplus;          /* index of T+                                  */
+    double  pminus[3];       /* vertex of T- opposite to the edge            */
+    double  pplus[3];        /* vertex of T+ opposite to the edge            */
+    double  length;          /* edge length (see FRICO_EDGE_LENGTH_*)        */
+    int64_t edge_index;      /* index in the sorted edge list                */
+    int64_t matrix_index;    /* row/column of Z                              */
+    int32_t has_interface;   /* 1 if the edge lies on a tagged curve         */
+    int32_t interface_tag;   /* that curve's tag                             */
+} frico_rwg;
+
+/* Mirrors frico::maxwell::config (src/emw_solver.h:41-53), plus GPU knobs. */
+typedef struct frico_gpu_options {
+    int32_t degree;          /* Dunavant degree, 0..20 (0 behaves as 1)      */
+    int32_t approx;          /* 1: compute_matrix_approx (-A)                */
+    int32_t force_symmetry;  /* 1: Z <- (Z + Z^T)/2 before the solve (-S)    */
+    int32_t precision;       /* FRICO_PREC_*                                 */
+    int32_t h_phase_mode;    /* FRICO_HPHASE_*                               */
+    int32_t max_refine_iters;/* mixed precision: refinement sweeps (<=0: 30) */
+    double  refine_tol;      /* mixed precision: stop at ||r||/||b|| <= tol (<=0: 1e-12) */
+    double  Z0;              /* reference impedance for gamma/SWR (-Z)       */
+    int32_t profile_kernels; /* 1: CUDA-event timing of every LU update GEMM */
+    int32_t reserved;
+} frico_gpu_options;
+
+/* Port values (src/emw_ana_antenna.h:31-38). */
+typedef struct frico_port_values {
+    frico_c128 voltage, current, power, impedance, gamma;
+    double     swr;
+} frico_port_values;
+
+/* Per-stage device times of the last calls, CUDA events on the context stream. */
+typedef struct frico_gpu_stats {
+    double fill_ms, rhs_ms, factor_ms, solve_ms, refine_ms, lump_ms, fields_ms;
+    int32_t refine_iters;
+    double  refine_residual;     /* final ||b - Z x|| / ||b|| (FP64)        */
+    int64_t n, ntri, nrhs;
+    int64_t green_evals;         /* Green-function evaluations of last fill */
+    int64_t kernel_launches;     /* kernels launched by this context so far */
+    int64_t gemm_launches;       /* LU trailing-update launches timed (profile_kernels) */
+    double  gemm_ms;             /* their summed CUDA-event time            */
+    double  gemm_flops;          /* their algorithmic real flops (8 m n k)  */
+} frico_gpu_stats;
+
+typedef struct frico_gpu_ctx frico_gpu_ctx;
+
+/* ---- host-side mesh front end (no device work) ------------------------
+ * Builds FRICO's connectivity and RWG table from a triangle soup, as
+ * load_from_gmsh + compute_connectivity + make_function_space do
+ * (src/input_gmsh.cpp:216-406, src/rwg_basis.cpp:27-68):
+ *   edges sorted by (min vertex, max vertex) and deduplicated; T- is the lower
+ *   triangle index; curves (1-D elements, tagged) that coincide with interior
+ *   edges become interfaces; unused vertices are compacted away.
+ * Inputs: nv vertices xyz[3*nv]; nt triangles tri[3*nt] (0-based vertex ids);
+ * ncurve tagged segments curve[2*ncurve], curve_tag[ncurve] (may be 0/NULL).
+ * Outputs: rwg[capacity], *n_rwg; rwg_edge_vertices[2*capacity] (the two
+ * compacted vertex ids of each RWG edge, may be NULL); vertices_out[3*nv]
+ * (compacted, may be NULL), *nv_out; tri_out[3*nt] (re-indexed, may be NULL).
+ * Errors: FRICO_GPU_EMESH for an edge shared by >2 triangles or a curve segment
+ * that is not an edge of any triangle; FRICO_GPU_EINVAL if capacity is short
+ * (then *n_rwg holds the size needed). */
+int frico_gpu_make_function_space(int64_t nv, const double* xyz,
+                                  int64_t nt, const int64_t* tri,
+                                  int64_t ncurve, const int64_t* curve, const int32_t* curve_tag,
+                                  int32_t edge_length_mode,
+                                  frico_rwg* rwg, int64_t capacity, int64_t* n_rwg,
+                                  int64_t* rwg_edge_vertices,
+                                  double* vertices_out, int64_t* nv_out, int64_t* tri_out);
+
+/* Delta-gap orientation signs (src/emw_solver.cpp:222-350). xyz/tri are the
+ * compacted mesh, tri_tag[nt] the surface tags, rwg[n] the RWG table and
+ * rwg_edge_vertices[2*n] the vertex ids of each RWG edge (as returned above).
+ * Writes signs[n] (only the feed entries are meaningful) and *applied = 1 when
+ * the reorientation ran (otherwise signs are all +1). */
+int frico_gpu_reorient_deltagap(int64_t nv, const double* xyz, const int64_t* tri,
+                                const int32_t* tri_tag, int64_t n, const frico_rwg* rwg,
+                                const int64_t* rwg_edge_vertices, int32_t n_itf,
+                                const int32_t* itf_tags, int32_t force,
+                                double* signs, int32_t* applied);
+
+/* ---- context ---------------------------------------------------------- */
+int frico_gpu_ctx_create(frico_gpu_ctx** ctx, int device, const frico_gpu_options* opt);
+int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx);
+int frico_gpu_set_options(frico_gpu_ctx* ctx, const frico_gpu_options* opt);
+const char* frico_gpu_last_error(frico_gpu_ctx* ctx);
+/* The CUDA stream (cudaStream_t) every kernel of this context runs on. */
+int frico_gpu_get_stream(frico_gpu_ctx* ctx, void** stream);
+
+/* Upload mesh + RWG table (the state FRICO keeps in `simulation`). */
+int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* xyz,
+                       int64_t nt, const int64_t* tri,
+                       int64_t n, const frico_rwg* rwg);
+
+/* compute_matrix / compute_matrix_approx at `freq` Hz. Z stays on the device;
+ * if Z_out != NULL it is also copied there (column-major, leading dim ldz >= n). */
+int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out, int64_t ldz);
+
+/* Set the right-hand-side count (columns of V); resets V to zero. */
+int frico_gpu_set_nrhs(frico_gpu_ctx* ctx, int32_t nrhs);
+/* update_rhs(delta_gap): V[:,col] += (-j l/(omega mu0)) V0 sign on feed edges.
+ * signs may be NULL (all +1). */
+int frico_gpu_rhs_delta_gap(frico_gpu_ctx* ctx, double freq, int32_t col,
+                            int32_t n_itf, const int32_t* itf_tags,
+                            frico_c128 V0, const double* signs);
+/* update_rhs(plane_wave): Dunavant-integrated <f, E_inc> / (-j omega mu0). */
+int frico_gpu_rhs_plane_wave(frico_gpu_ctx* ctx, double freq, int32_t col,
+                             double theta, double phi, frico_c128 Etheta, frico_c128 Ephi);
+/* Upload / download V (n x nrhs, column-major, ld >= n). */
+int frico_gpu_set_rhs(frico_gpu_ctx* ctx, int32_t nrhs, const frico_c128* V, int64_t ldv);
+int frico_gpu_get_rhs(frico_gpu_ctx* ctx, frico_c128* V, int64_t ldv);
+
+/* solve_general: factor the resident Z (LAPACK zgetrf semantics, partial
+ * pivoting by max |re|+|im|) and solve Z I = V for all nrhs columns.
+ * *info: 0, or k>0 for an exactly-zero pivot in column k (1-based), as zgetrf.
+ * I_out (n x nrhs, ld ldi) optional. With FRICO_PREC_MIXED the factorisation
+ * is complex64 and the currents are refined against the FP64 Z. */
+int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ldi, int32_t* info);
+/* Download the LU factors (FP64 path: LAPACK layout) and 1-based ipiv. */
+int frico_gpu_get_factors(frico_gpu_ctx* ctx, frico_c128* LU, int64_t ld, int32_t* ipiv);
+
+/* run_context's current lumping for RHS column `col` (src/emw_solver.h:137-164):
+ * tri_AJ[nt*3] (row-major rows of 3), tri_AdivJ[nt], tri_J[nt*3]; all optional. */
+int frico_gpu_lump_currents(frico_gpu_ctx* ctx, int32_t col,
+                            frico_c128* tri_AJ, frico_c128* tri_AdivJ, frico_c128* tri_J);
+
+/* eval_fields at npts points P[3*npts] for RHS column `col` (after lumping).
+ * E[3*npts], H[3*npts] (row-major rows of 3). */
+int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t npts, const double* P,
+                          frico_c128* E, frico_c128* H);
+
+/* compute_port_values for the delta gap on `itf_tags` (RHS column `col`). */
+int frico_gpu_port_values(frico_gpu_ctx* ctx, int32_t col, int32_t n_itf,
+                          const int32_t* itf_tags, frico_c128 V0, const double* signs,
+                          frico_port_values* out);
+/* compute_gain: 360 gains on `plane` at distance R for input power pwr. */
+int frico_gpu_gain(frico_gpu_ctx* ctx, int32_t col, double pwr, double R,
+                   int32_t plane, double* G360);
+/* Bistatic RCS (src/emw_ana_bistatic_rcs.cpp:102-117): out[359*4] rows
+ * {VV_theta, HH_theta, VV_phi, HH_phi} for angles 0..358 degrees. */
+int frico_gpu_bistatic_rcs(frico_gpu_ctx* ctx, int32_t col, double R, double* out);
+/* sigma_VV / sigma_HH at arbitrary (theta, phi) directions, radius R:
+ * out[2*npts] = {VV, HH} per direction. */
+int frico_gpu_rcs_points(frico_gpu_ctx* ctx, int32_t col, double R, int64_t npts,
+                         const double* theta, const double* phi, double* out);
+
+int frico_gpu_last_stats(frico_gpu_ctx* ctx, frico_gpu_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FRICO_GPU_H */

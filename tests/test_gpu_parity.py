@@ -1,0 +1,235 @@
+"""GPU parity: libfrico_gpu (through its C-ABI) against the CPU oracle.
+
+Tolerances (FP64 drop-in): Z entries 1e-10 relative, input impedance,
+currents and fields 1e-9 relative. Mixed precision: 1e-6 relative on Zin and
+far fields after FP64 refinement.
+"""
+import numpy as np
+import pytest
+
+from frico_gb300 import meshes
+from frico_gb300.solver import DeltaGap, PlaneWave, Simulation
+
+pytestmark = pytest.mark.gpu
+
+Z_TOL = 1e-10
+OUT_TOL = 1e-9
+MIXED_TOL = 1e-6
+
+
+def rel_entrywise(a, b, floor_frac=1e-8):
+    """max |a-b| / max(|b|, floor) with floor = floor_frac * max|b|."""
+    b_abs = np.abs(b)
+    den = np.maximum(b_abs, floor_frac * b_abs.max())
+    return float((np.abs(a - b) / den).max())
+
+
+def rel_norm(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def strip():
+    return meshes.strip_dipole()
+
+
+@pytest.fixture(scope="module")
+def sphere2():
+    return meshes.icosphere(2)
+
+
+def oracle_for(mesh, **kw):
+    from oracle import Oracle
+    return Oracle(mesh, **kw)
+
+
+@pytest.mark.parametrize("approx", [False, True])
+def test_fill_strip(gpu_lib, strip, approx):
+    o = oracle_for(strip)
+    Zr = o.compute_matrix(300e6, approx=approx)
+    sim = Simulation(strip, approx_matrix=approx)
+    Z = sim.compute_matrix(300e6, download=True)
+    assert rel_entrywise(Z, Zr) < Z_TOL
+    if approx:
+        assert np.abs(Z - Z.T).max() < 1e-14 * np.abs(Z).max()
+
+
+@pytest.mark.parametrize("degree", [0, 2, 3, 4, 7])
+def test_fill_degrees(gpu_lib, degree):
+    m = meshes.icosphere(1)
+    o = oracle_for(m, degree=degree)
+    Zr = o.compute_matrix(450e6)
+    sim = Simulation(m, degree=degree)
+    Z = sim.compute_matrix(450e6, download=True)
+    assert rel_entrywise(Z, Zr) < Z_TOL
+
+
+def test_fill_sphere_l3(gpu_lib):
+    m = meshes.icosphere(3)
+    o = oracle_for(m)
+    Zr = o.compute_matrix(450e6)
+    sim = Simulation(m)
+    Z = sim.compute_matrix(450e6, download=True)
+    assert Z.shape == (1920, 1920)
+    assert rel_entrywise(Z, Zr) < Z_TOL
+
+
+def test_antenna_strip_fp64(gpu_lib, strip):
+    f = 300e6
+    o = oracle_for(strip)
+    Zr = o.compute_matrix(f)
+    Vr = o.rhs_delta_gap(f, [meshes.FEED_TAG])
+    Ir = o.solve(Zr, Vr)
+    pr = o.port_values(Ir, o.rwg(), [meshes.FEED_TAG])
+    AJr, ADr, Jr = o.lump(f, Ir)
+    sim = Simulation(strip)
+    dg = DeltaGap((meshes.FEED_TAG,))
+    sim.compute_matrix(f)
+    sim.set_nrhs(1)
+    sim.update_rhs(f, dg)
+    V = sim.get_rhs()[:, 0]
+    assert rel_entrywise(V, Vr) < 1e-14 if np.abs(Vr).max() > 0 else True
+    I = sim.solve()[:, 0]
+    assert rel_norm(I, Ir) < OUT_TOL
+    pv = sim.port_values(dg)
+    assert abs(pv["impedance"] - pr["impedance"]) / abs(pr["impedance"]) < OUT_TOL
+    AJ, AD, J = sim.lump_currents()
+    assert rel_norm(AJ, AJr) < OUT_TOL and rel_norm(AD, ADr) < OUT_TOL and rel_norm(J, Jr) < OUT_TOL
+    T, P, pts = meshes.far_field_grid(10.0, 6.0)
+    E, H = sim.eval_fields(pts)
+    Er, Hr = o.eval_fields(pts)
+    assert rel_norm(E, Er) < OUT_TOL and rel_norm(H, Hr) < OUT_TOL
+    for plane in (0, 1, 2):
+        G = sim.compute_gain(pv["power"].real, 10.0, plane)
+        Gr = o.gain(pr["power"].real, 10.0, plane)
+        assert np.max(np.abs(G - Gr) / np.abs(Gr).max()) < OUT_TOL
+
+
+def test_scatter_sphere_fp64(gpu_lib, sphere2):
+    f = 450e6
+    o = oracle_for(sphere2)
+    Zr = o.compute_matrix(f)
+    Vr = o.rhs_plane_wave(f, 0.0, 0.0, 1.0, 0.0)
+    Ir = o.solve(Zr, Vr)
+    o.lump(f, Ir)
+    sim = Simulation(sphere2)
+    sim.compute_matrix(f)
+    sim.set_nrhs(1)
+    sim.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+    assert rel_norm(sim.get_rhs()[:, 0], Vr) < 1e-13
+    I = sim.solve()[:, 0]
+    assert rel_norm(I, Ir) < OUT_TOL
+    sig = sim.bistatic_rcs(10.0)
+    sigr = o.bistatic_rcs(10.0)
+    assert np.max(np.abs(sig - sigr)) / np.abs(sigr).max() < OUT_TOL
+    T, P, _ = meshes.bistatic_cuts(10.0)
+    s2 = sim.rcs_points(10.0, T, P)
+    s2r = o.rcs(10.0, T, P)
+    assert np.max(np.abs(s2 - s2r)) / np.abs(s2r).max() < OUT_TOL
+
+
+def test_mixed_precision_sphere(gpu_lib):
+    m = meshes.icosphere(3)
+    f = 450e6
+    o = oracle_for(m)
+    Zr = o.compute_matrix(f)
+    Vr = o.rhs_plane_wave(f, 0.0, 0.0, 1.0, 0.0)
+    Ir = o.solve(Zr, Vr)
+    o.lump(f, Ir)
+    T, P, pts = meshes.bistatic_cuts(10.0)
+    Er, _ = o.eval_fields(pts)
+    sim = Simulation(m, precision="mixed")
+    sim.compute_matrix(f)
+    sim.set_nrhs(1)
+    sim.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+    I = sim.solve()[:, 0]
+    st = sim.stats()
+    assert st["refine_iters"] >= 1 and st["refine_residual"] < 1e-10
+    assert rel_norm(I, Ir) < MIXED_TOL
+    E, _ = sim.eval_fields(pts)
+    assert rel_norm(E, Er) < MIXED_TOL
+
+
+def test_mixed_strip_zin(gpu_lib, strip):
+    f = 300e6
+    o = oracle_for(strip)
+    Zr = o.compute_matrix(f)
+    Ir = o.solve(Zr, o.rhs_delta_gap(f, [meshes.FEED_TAG]))
+    pr = o.port_values(Ir, o.rwg(), [meshes.FEED_TAG])
+    sim = Simulation(strip, precision="mixed")
+    dg = DeltaGap((meshes.FEED_TAG,))
+    sim.run_context(f, dg)
+    pv = sim.port_values(dg)
+    assert abs(pv["impedance"] - pr["impedance"]) / abs(pr["impedance"]) < MIXED_TOL
+
+
+def test_multi_rhs_and_factors(gpu_lib, sphere2):
+    """Several right-hand sides share one factorisation; factors match LAPACK's solution."""
+    f = 450e6
+    o = oracle_for(sphere2)
+    Zr = o.compute_matrix(f)
+    rng = np.random.default_rng(5)
+    B = rng.standard_normal((o.n, 5)) + 1j * rng.standard_normal((o.n, 5))
+    Xr = o.solve(Zr, B)
+    sim = Simulation(sphere2)
+    sim.compute_matrix(f)
+    sim.set_rhs(B)
+    X = sim.solve()
+    assert rel_norm(X, Xr) < OUT_TOL
+    LU, ipiv = sim.get_factors()
+    assert ipiv.min() >= 1 and ipiv.max() <= o.n
+    L = np.tril(LU, -1) + np.eye(o.n)
+    U = np.triu(LU)
+    PA = Zr.copy()
+    for k, p in enumerate(ipiv - 1):
+        PA[[k, p]] = PA[[p, k]]
+    assert rel_norm(L @ U, PA) < 1e-12
+
+
+def test_singular_matrix_info(gpu_lib):
+    """The xy-hypot edge length makes vertical edges zero-length: Z gets zero
+    rows/columns and zgetrf reports the first zero pivot; so must the GPU."""
+    m = meshes.strip_dipole()
+    m.vertices = m.vertices[:, [0, 2, 1]].copy()   # strip in the xz-plane: transverse edges vertical
+    o = oracle_for(m)
+    Zr = o.compute_matrix(300e6)
+    from scipy.linalg import lapack
+    _, _, info_ref = lapack.zgetrf(Zr)
+    assert info_ref > 0
+    sim = Simulation(m)
+    sim.compute_matrix(300e6)
+    sim.set_nrhs(1)
+    sim.update_rhs(300e6, DeltaGap((meshes.FEED_TAG,)))
+    from frico_gb300 import FricoError
+    with pytest.raises(FricoError) as e:
+        sim.solve()
+    assert e.value.code == -2
+    import ctypes
+    info = ctypes.c_int32(0)
+    rc = sim.lib.frico_gpu_solve(sim.ctx, None, sim.n, ctypes.byref(info))
+    assert rc == -2 and info.value == info_ref
+
+
+def test_true_edge_length_invariance(gpu_lib, sphere2):
+    """Physical outputs do not depend on the edge-length convention."""
+    f = 450e6
+    out = []
+    for mode in ("xy", "true"):
+        sim = Simulation(sphere2, edge_length=mode)
+        sim.run_context(f, PlaneWave(0.3, 0.2, 1.0, 0.0))
+        out.append(sim.bistatic_rcs(10.0))
+    assert np.max(np.abs(out[0] - out[1])) / np.abs(out[1]).max() < 1e-7
+
+
+def test_error_paths(gpu_lib, strip):
+    from frico_gb300 import FricoError
+    sim = Simulation(strip)
+    with pytest.raises(FricoError) as e:
+        sim.solve()
+    assert e.value.code == -6
+    with pytest.raises(FricoError) as e:
+        sim.set_options(degree=21)
+    assert e.value.code == -1
+    with pytest.raises(FricoError) as e:
+        sim.compute_matrix(-1.0)
+    assert e.value.code == -1
