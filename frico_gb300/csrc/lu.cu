@@ -553,7 +553,15 @@ static int lu_factor_impl(frico_gpu_ctx* ctx, cplx<R>* A) {
     int dev_sms = 0, max_smem = 0;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    cudaFuncSetAttribute(k_panel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    {
+        // dynamic limit = opt-in limit minus the kernel's static shared memory
+        cudaFuncAttributes fa;
+        if ((rc = cuda_check(ctx, cudaFuncGetAttributes(&fa, k_panel<R>), "panel attributes"))) return rc;
+        max_smem -= int(fa.sharedSizeBytes);
+        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(k_panel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      max_smem), "panel smem attribute")))
+            return rc;
+    }
     const size_t trsm_smem = sizeof(C) * (kNB * kNB + 32 * kNB);
     cudaFuncSetAttribute(k_trsm_lower_unit<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(trsm_smem));
 

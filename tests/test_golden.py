@@ -1,0 +1,139 @@
+"""Pins: the oracle and the GPU library against golden vectors produced by
+FRICO's own sources (tests/golden/make_golden.py), plus a direct comparison
+with the in-place reference build where it exists."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from frico_gb300 import meshes
+
+G = Path(__file__).resolve().parent / "golden"
+FEED = [meshes.FEED_TAG]
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(b).max())
+
+
+def load(name):
+    return np.load(G / f"{name}.npz")
+
+
+# ------------------------------------------------------------------ oracle (CPU)
+def test_oracle_quadrature_golden():
+    from oracle import dunavant
+    g = load("quadrature")
+    for d in range(0, 21):
+        q = dunavant(d, g["p0"], g["p1"], g["p2"])
+        ref = g[f"deg{d}"]
+        assert q.shape == ref.shape
+        assert np.abs(q - ref).max() <= 1e-15 * max(1.0, np.abs(ref).max())
+
+
+def test_oracle_strip_golden():
+    from oracle import Oracle
+    g = load("strip")
+    o = Oracle(meshes.strip_dipole())
+    assert np.array_equal(o.rwg(), g["rwg"])
+    f = float(g["freq"])
+    assert rel(o.compute_matrix(f), g["Z"]) < 1e-14
+    assert rel(o.compute_matrix(f, approx=True), g["Z_approx"]) < 1e-14
+    V = o.rhs_delta_gap(f, FEED)
+    assert rel(V, g["V"]) < 1e-15
+    I = o.solve(o.compute_matrix(f), V)
+    assert rel(I, g["I"]) < 1e-12
+    AJ, AD, J = o.lump(f, g["I"])
+    assert rel(AJ, g["AJ"]) < 1e-14 and rel(AD, g["AdivJ"]) < 1e-14 and rel(J, g["J"]) < 1e-14
+    E, H = o.eval_fields(g["points"])
+    assert rel(E, g["E"]) < 1e-13 and rel(H, g["H"]) < 1e-13
+    pv = o.port_values(g["I"], o.rwg(), FEED)
+    assert abs(pv["impedance"] - g["port"][2]) / abs(g["port"][2]) < 1e-14
+    for p in range(3):
+        assert rel(o.gain(pv["power"].real, 10.0, p), g["gains"][p]) < 1e-13
+
+
+def test_oracle_sphere_golden():
+    from oracle import Oracle
+    g = load("sphere1")
+    m = meshes.icosphere(1)
+    f = float(g["freq"])
+    for d in (2, 5):
+        assert rel(Oracle(m, degree=d).compute_matrix(f), g[f"Z_deg{d}"]) < 1e-14
+    o = Oracle(m)
+    assert rel(o.rhs_plane_wave(f, 0.0, 0.0, 1.0, 0.0), g["V"]) < 1e-14
+    o.lump(f, g["I"])
+    assert rel(o.bistatic_rcs(10.0), g["bistatic"]) < 1e-12
+
+
+def test_oracle_bowtie_golden():
+    from oracle import Oracle
+    g = load("bowtie")
+    o = Oracle(meshes.bowtie(6, 4))
+    assert np.array_equal(o.rwg(), g["rwg"])
+    s = o.reorient(FEED, force=True)
+    feed = g["signs"] != 0
+    assert np.array_equal(s[feed], g["signs"][feed])
+    assert rel(o.rhs_delta_gap(float(g["freq"]), FEED, 1.0, s), g["V"]) < 1e-15
+
+
+def test_oracle_against_reference_build():
+    """Direct pin against FRICO compiled in place (only where the checkout exists)."""
+    import ref_frico
+    if not ref_frico.available():
+        pytest.skip("reference build not present on this machine")
+    from oracle import Oracle
+    m = meshes.icosphere(2)
+    r = ref_frico.RefFrico(m, degree=3)
+    o = Oracle(m, degree=3)
+    assert np.array_equal(r.rwg(), o.rwg())
+    assert np.array_equal(r.compute_matrix(450e6), o.compute_matrix(450e6))
+    m = meshes.bowtie(8, 5)
+    m.tri_tags = np.ones_like(m.tri_tags)    # one surface: T+.tag <= T-.tag triggers the reorientation
+    r, o = ref_frico.RefFrico(m), Oracle(m)
+    assert np.array_equal(r.rwg(), o.rwg())
+    a, b = r.reorient(FEED), o.reorient(FEED)
+    assert a is not None and b is not None
+    feed = a != 0
+    assert feed.sum() == 5 and np.array_equal(a[feed], b[feed])
+
+
+# ------------------------------------------------------------------ GPU vs golden
+@pytest.mark.gpu
+def test_gpu_strip_golden(gpu_lib):
+    from frico_gb300.solver import DeltaGap, Simulation
+    g = load("strip")
+    f = float(g["freq"])
+    sim = Simulation(meshes.strip_dipole())
+    assert rel(sim.compute_matrix(f, download=True), g["Z"]) < 1e-10
+    dg = DeltaGap(tuple(FEED))
+    sim.set_nrhs(1)
+    sim.update_rhs(f, dg)
+    I = sim.solve()[:, 0]
+    assert rel(I, g["I"]) < 1e-9
+    pv = sim.port_values(dg)
+    assert abs(pv["impedance"] - g["port"][2]) / abs(g["port"][2]) < 1e-9
+    E, H = sim.eval_fields(g["points"])
+    assert rel(E, g["E"]) < 1e-9 and rel(H, g["H"]) < 1e-9
+    for p in range(3):
+        assert rel(sim.compute_gain(pv["power"].real, 10.0, p), g["gains"][p]) < 1e-9
+    sa = Simulation(meshes.strip_dipole(), approx_matrix=True)
+    assert rel(sa.compute_matrix(f, download=True), g["Z_approx"]) < 1e-10
+
+
+@pytest.mark.gpu
+def test_gpu_sphere_golden(gpu_lib):
+    from frico_gb300.solver import PlaneWave, Simulation
+    g = load("sphere1")
+    m = meshes.icosphere(1)
+    f = float(g["freq"])
+    for d in (2, 5):
+        assert rel(Simulation(m, degree=d).compute_matrix(f, download=True), g[f"Z_deg{d}"]) < 1e-10
+    sim = Simulation(m)
+    sim.run_context(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+    assert rel(sim.get_rhs()[:, 0], g["V"]) < 1e-13
+    assert rel(sim.bistatic_rcs(10.0), g["bistatic"]) < 1e-9
+    for prec in ("mixed",):
+        s2 = Simulation(m, precision=prec)
+        s2.run_context(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+        assert rel(s2.bistatic_rcs(10.0), g["bistatic"]) < 1e-6
