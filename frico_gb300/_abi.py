@@ -18,6 +18,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 EDGE_LENGTH_XY, EDGE_LENGTH_TRUE = 0, 1
 HPHASE_COMPAT, HPHASE_PHYSICAL = 0, 1
 GAIN_XY, GAIN_YZ, GAIN_XZ = 0, 1, 2
+GEMM_AUTO, GEMM_SIMT, GEMM_TC = 0, 1, 2
 
 # numpy mirror of frico_rwg (112 bytes)
 RWG_DTYPE = np.dtype([
@@ -36,7 +37,7 @@ class Options(C.Structure):
     _fields_ = [("degree", C.c_int32), ("approx", C.c_int32), ("force_symmetry", C.c_int32),
                 ("precision", C.c_int32), ("h_phase_mode", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("refine_tol", C.c_double), ("Z0", C.c_double), ("profile_kernels", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("gemm_engine", C.c_int32)]
 
 
 class PortValues(C.Structure):
@@ -81,6 +82,7 @@ PROTOTYPES = {
     "frico_gpu_bistatic_rcs": [P, I32, D, P],
     "frico_gpu_rcs_points": [P, I32, D, I64, P, P, P],
     "frico_gpu_last_stats": [P, P],
+    "frico_gpu_debug_cgemm": [P, I32, I32, I32, P, P, P, I32],
 }
 
 _lib = None

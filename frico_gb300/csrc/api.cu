@@ -69,6 +69,8 @@ static int check_options(frico_gpu_ctx* ctx, const frico_gpu_options* o) {
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown precision");
     if (o->h_phase_mode != FRICO_HPHASE_COMPAT && o->h_phase_mode != FRICO_HPHASE_PHYSICAL)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown h_phase_mode");
+    if (o->gemm_engine < FRICO_GEMM_AUTO || o->gemm_engine > FRICO_GEMM_TC)
+        return set_err(ctx, FRICO_GPU_EINVAL, "unknown gemm_engine");
     return FRICO_GPU_OK;
 }
 
@@ -121,7 +123,8 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->rwg_itf, &ctx->tri_bf,   &ctx->gtab,     &ctx->smom,      &ctx->basis_aux, &ctx->z64,
                       &ctx->z32,     &ctx->lu,       &ctx->ipiv,     &ctx->perm,      &ctx->panel_ws, &ctx->status,
                       &ctx->rhs,     &ctx->sol,      &ctx->rwork,    &ctx->rwork32,   &ctx->dwork32, &ctx->norms,
-                      &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out};
+                      &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
+                      &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -549,6 +552,39 @@ extern "C" int frico_gpu_rcs_points(frico_gpu_ctx* ctx, int32_t col, double R, i
     if (rc) return rc;
     for (int64_t i = 0; i < npts; i++) rcs_from_E(&E[3 * i], theta[i], phi[i], R, &out[2 * i], &out[2 * i + 1]);
     return FRICO_GPU_OK;
+}
+
+extern "C" int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, int32_t k, const frico_c64* A,
+                                     const frico_c64* B, frico_c64* C, int32_t engine) {
+    FRICO_CTX_CHECK(ctx);
+    if (m <= 0 || n <= 0 || k <= 0 || !A || !B || !C) return set_err(ctx, FRICO_GPU_EINVAL, "debug_cgemm: bad args");
+    if (engine != FRICO_GEMM_SIMT && engine != FRICO_GEMM_TC)
+        return set_err(ctx, FRICO_GPU_EINVAL, "debug_cgemm: engine must be SIMT or TC");
+    if (engine == FRICO_GEMM_TC && !gemm_tc_available(ctx))
+        return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
+    int rc;
+    if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
+    if ((rc = cuda_check(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(DeviceStatus), ctx->stream), "status")))
+        return rc;
+    const size_t sa = size_t(m) * k, sb = size_t(k) * n, sc = size_t(m) * n;
+    DevBuf buf;
+    if ((rc = ensure(ctx, buf, sizeof(float2) * (sa + sb + sc)))) return rc;
+    float2* dA = (float2*)buf.p;
+    float2* dB = dA + sa;
+    float2* dC = dB + sb;
+    rc = cuda_check(ctx, cudaMemcpyAsync(dA, A, sizeof(float2) * sa, cudaMemcpyHostToDevice, ctx->stream), "A");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(dB, B, sizeof(float2) * sb, cudaMemcpyHostToDevice, ctx->stream), "B");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(dC, C, sizeof(float2) * sc, cudaMemcpyHostToDevice, ctx->stream), "C");
+    if (!rc)
+        rc = engine == FRICO_GEMM_TC ? gemm_update_tc(ctx, dC, m, dA, m, dB, k, m, n, k, nullptr)
+                                     : gemm_update_simt32(ctx, dC, m, dA, m, dB, k, m, n, k);
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(C, dC, sizeof(float2) * sc, cudaMemcpyDeviceToHost, ctx->stream), "C");
+    DeviceStatus hs{};
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(&hs, ctx->status.p, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream), "st");
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    release(buf);
+    if (!rc && hs.err == FRICO_DEV_ERR_TIMEOUT) rc = set_err(ctx, FRICO_GPU_ETIMEOUT, "tensor-core GEMM wait timed out");
+    return rc;
 }
 
 extern "C" int frico_gpu_last_stats(frico_gpu_ctx* ctx, frico_gpu_stats* stats) {

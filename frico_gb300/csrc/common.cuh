@@ -120,6 +120,9 @@ struct frico_gpu_ctx {
     frico::DevBuf lu, ipiv, perm, panel_ws, status;
     int32_t nrhs = 0;
     frico::DevBuf rhs, sol, rwork, rwork32, dwork32, norms;
+    frico::DevBuf dinv, trsv_flags;  // inverted diagonal blocks, chain flags + ticket
+    frico::DevBuf tc_ws;             // split operands of the tensor-core trailing update
+    int trsv_epoch = 0;
     bool solved = false;
 
     // post-processing
@@ -165,8 +168,17 @@ int symmetrize(frico_gpu_ctx* ctx);                           // fill.cu
 int lu_factor_fp64(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_factor_fp32(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb);   // lu.cu
-int lu_solve_fp32(frico_gpu_ctx* ctx, float2* B, int nrhs, int64_t ldb);    // lu.cu
 int refine_solve(frico_gpu_ctx* ctx);                         // lu.cu
+int trsv_prepare_fp64(frico_gpu_ctx* ctx);                    // trsv.cu
+int trsv_prepare_fp32(frico_gpu_ctx* ctx);                    // trsv.cu
+int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw);  // trsv.cu
+int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw);   // trsv.cu
+int trsv_check(frico_gpu_ctx* ctx);                           // trsv.cu
+bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
+int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
+                   const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev);  // gemm_tc.cu
+int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
+                       const float2* U, int64_t ldu, int m, int n, int k);  // lu.cu
 int rhs_delta_gap(frico_gpu_ctx* ctx, double freq, int col, int n_itf, const int32_t* tags,
                   double2 V0, const double* signs);           // fields.cu
 int rhs_plane_wave(frico_gpu_ctx* ctx, double freq, int col, double theta, double phi,

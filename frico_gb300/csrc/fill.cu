@@ -121,12 +121,18 @@ __global__ void k_build_quadrature(int64_t nt, const double* __restrict__ xyz,
 //   mode 0 (degree 1): rho at the single quadrature point, q - p_free
 //   mode 2 (MOM3D):    rho at the barycentre, c - p_free
 // `v_m`/`v_p` = p_free - centroid, the offsets the moment expansion needs.
+// The factors of a block are regrouped per half-basis (RWG i on side s), so
+// that an entry costs a few FP64 FMAs per block:
+//   prodl * w_p w_q / (A_is A_jt) = (q_is w_p)(q_jt w_q),  q = l / (2 sqrt(pi) A)
+//   1/4 rho_is.rho_jt - 1/k^2     = rho'_is.rho'_jt - 1/k^2,  rho' = rho / 2
+// (the same products as src/emw_solver.cpp:81-93, associated differently).
 struct BasisAsm {
     int32_t itm, itp;
-    double len, am, ap;
-    double a_m[3], a_p[3];
-    double v_m[3], v_p[3];
-    double w_m, w_p;
+    double len;
+    double a_m[3], a_p[3];   // rho'/2 at the degree-1 point (mode 0) or barycentre (mode 2), halved
+    double v_m[3], v_p[3];   // p_free - centroid (moment expansion)
+    double q_m, q_p;         // l / (2 sqrt(pi) A)
+    double h_m, h_p;         // q * (degree-1 quadrature weight)
 };
 
 __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo,
@@ -138,24 +144,26 @@ __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo
     b.itm = rw.itm[i];
     b.itp = rw.itp[i];
     b.len = rw.len[i];
-    b.am = rw.am[i];
-    b.ap = rw.ap[i];
+    const double am = rw.am[i], ap = rw.ap[i];
     const double* qm = qp + 4 * nq * int64_t(b.itm);
     const double* qpp = qp + 4 * nq * int64_t(b.itp);
     for (int d = 0; d < 3; d++) {
         double vm = rw.vm[3 * i + d], vp = rw.vp[3 * i + d];
         if (mode == 2) {
-            b.a_m[d] = geo[b.itm].c[d] - vm;
-            b.a_p[d] = geo[b.itp].c[d] - vp;
+            b.a_m[d] = 0.5 * (geo[b.itm].c[d] - vm);
+            b.a_p[d] = 0.5 * (geo[b.itp].c[d] - vp);
         } else {
-            b.a_m[d] = qm[d] - vm;
-            b.a_p[d] = qpp[d] - vp;
+            b.a_m[d] = 0.5 * (qm[d] - vm);
+            b.a_p[d] = 0.5 * (qpp[d] - vp);
         }
         b.v_m[d] = vm - geo[b.itm].c[d];
         b.v_p[d] = vp - geo[b.itp].c[d];
     }
-    b.w_m = qm[3];
-    b.w_p = qpp[3];
+    const double s = 0.5 * b.len / sqrt(M_PI);
+    b.q_m = s / am;
+    b.q_p = s / ap;
+    b.h_m = b.q_m * qm[3];
+    b.h_p = b.q_p * qpp[3];
     out[i] = b;
 }
 
@@ -204,6 +212,67 @@ __global__ void k_gtab_approx(int64_t nt, const TriGeo* __restrict__ geo, double
         g = make_double2(0.25 * (sqrt_4pi / sa) * M_1_PI, 0.25 * (-k) * M_1_PI);
     }
     G[a * nt + b] = g;
+}
+
+// Symmetric tile form of the two single-point tables above: g(a,b) = g(b,a),
+// so a CTA evaluates the 32x32 pairs of tile (ta, tb), ta <= tb, and stores
+// the tile and its transpose (both coalesced, through shared memory).
+// APPROX = 0: degree-1 points, g = exp(-jkR)/R, zero on the diagonal (never read).
+// APPROX = 1: barycentres, g = exp(-jkR)/(4 pi R), MOM3D self term on the diagonal.
+template <int APPROX>
+__global__ void __launch_bounds__(256) k_gtab_sym(int64_t nt, const QPoint* __restrict__ qp,
+                                                 const TriGeo* __restrict__ geo, double k, double2* __restrict__ G) {
+    __shared__ double pa[32][3], pb[32][3];
+    __shared__ double2 tile[32][33];
+    // map the linear block index onto the upper-triangular tile pairs
+    const int64_t T = (nt + 31) / 32;
+    int64_t lin = blockIdx.x, ta = 0;
+    while (lin >= T - ta) { lin -= T - ta; ta++; }
+    const int64_t tb = ta + lin;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    if (threadIdx.x < 64) {
+        int which = threadIdx.x >> 5, q = threadIdx.x & 31;
+        int64_t t = (which ? tb : ta) * 32 + q;
+        double* dst = which ? pb[q] : pa[q];
+        if (t < nt) {
+            if (APPROX) {
+                dst[0] = geo[t].c[0]; dst[1] = geo[t].c[1]; dst[2] = geo[t].c[2];
+            } else {
+                QPoint p = qp[t];
+                dst[0] = p.x; dst[1] = p.y; dst[2] = p.z;
+            }
+        } else {
+            dst[0] = dst[1] = dst[2] = 0.0;
+        }
+    }
+    __syncthreads();
+    const double sqrt_4pi = sqrt(4 * M_PI);
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t a = ta * 32 + r, b = tb * 32 + tx;
+        double2 g = make_double2(0.0, 0.0);
+        if (a < nt && b < nt) {
+            if (a != b) {
+                double dx = pa[r][0] - pb[tx][0], dy = pa[r][1] - pb[tx][1], dz = pa[r][2] - pb[tx][2];
+                double r2 = dx * dx + dy * dy + dz * dz;
+                double R = sqrt(r2);
+                double s, c;
+                sincos(k * R, &s, &c);
+                double inv = APPROX ? 1.0 / (4.0 * M_PI * R) : 1.0 / R;
+                g = make_double2(c * inv, -s * inv);
+            } else if (APPROX) {
+                double sa = sqrt(geo[a].area);
+                g = make_double2(0.25 * (sqrt_4pi / sa) * M_1_PI, 0.25 * (-k) * M_1_PI);
+            }
+            G[a * nt + b] = g;
+        }
+        tile[r][tx] = g;
+    }
+    if (ta == tb) return;
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t a = tb * 32 + r, b = ta * 32 + tx;   // transposed tile
+        if (a < nt && b < nt) G[a * nt + b] = tile[tx][r];
+    }
 }
 
 // Moments of g over point sets P (test, about ca) and Q (source, about cb):
@@ -302,43 +371,40 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs A) {
     const BasisAsm bi = A.bas[i];
     const BasisAsm bj = A.bas[j];
     double2 entry = make_double2(0.0, 0.0);
-    const double prodl = 0.25 * bi.len * bj.len * M_1_PI;
     const double lilj = bi.len * bj.len;
+    const double mk = -A.inv_ksq;
 #pragma unroll
     for (int blk = 0; blk < 4; blk++) {
         const int s = blk >> 1, t = blk & 1;  // order --, -+, +-, ++
         const int32_t ta = s ? bi.itp : bi.itm;
         const int32_t tb = t ? bj.itp : bj.itm;
-        const double ai = s ? bi.ap : bi.am;
-        const double aj = t ? bj.ap : bj.am;
         const double* vi = s ? bi.a_p : bi.a_m;
         const double* vj = t ? bj.a_p : bj.a_m;
         const double* oi = s ? bi.v_p : bi.v_m;
         const double* oj = t ? bj.v_p : bj.v_m;
         double2 c;
         if (MODE == 2) {
-            // src/emw_solver.cpp:181-215
+            // src/emw_solver.cpp:181-215: l_i l_j (1/4 rho.rho - 1/k^2) G
             double2 g = A.G[int64_t(ta) * A.nt + tb];
-            double rho = vi[0] * vj[0] + vi[1] * vj[1] + vi[2] * vj[2];
-            double2 d = csub(cscale(g, 0.25 * rho), cscale(g, A.inv_ksq));
-            c = cscale(d, lilj);
+            double f = lilj * fma(vi[0], vj[0], fma(vi[1], vj[1], fma(vi[2], vj[2], mk)));
+            c = cscale(g, f);
         } else {
-            const double inv_AA = 1. / (ai * aj);
             int split = (tb == bi.itm) ? 0 : (tb == bi.itp) ? 1 : -1;
+            const double qq = (s ? bi.q_p : bi.q_m) * (t ? bj.q_p : bj.q_m);
             if (split >= 0) {
                 const double2* m = A.S + (i * 4 + 2 * s + split) * 8;
                 double2 F = moment_block(m, 1, oi, oj, A.inv_ksq);
-                c = cscale(F, prodl * inv_AA);
+                c = cscale(F, qq);
             } else if (MODE == 0) {
-                // src/emw_solver.cpp:85-94
-                double v = 0.25 * (vi[0] * vj[0] + vi[1] * vj[1] + vi[2] * vj[2]);
-                double w = (s ? bi.w_p : bi.w_m) * (t ? bj.w_p : bj.w_m) * inv_AA;
+                // src/emw_solver.cpp:85-94: prodl w (1/4 rho.rho - 1/k^2) g
+                double hh = (s ? bi.h_p : bi.h_m) * (t ? bj.h_p : bj.h_m);
+                double f = hh * fma(vi[0], vj[0], fma(vi[1], vj[1], fma(vi[2], vj[2], mk)));
                 double2 g = A.G[int64_t(ta) * A.nt + tb];
-                c = cscale(g, prodl * w * (v - A.inv_ksq));
+                c = cscale(g, f);
             } else {
                 int64_t plane = A.nt * A.nt;
                 double2 F = moment_block(A.G + int64_t(ta) * A.nt + tb, plane, oi, oj, A.inv_ksq);
-                c = cscale(F, prodl * inv_AA);
+                c = cscale(F, qq);
             }
         }
         entry = (s == t) ? cadd(entry, c) : csub(entry, c);
@@ -458,12 +524,14 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
                                                            (BasisAsm*)ctx->basis_aux.p);
     dim3 gt(unsigned((nt + 127) / 128), unsigned(nt));
     double2* G = (double2*)ctx->gtab.p;
+    const int64_t T = (nt + 31) / 32;
+    const unsigned sym_blocks = unsigned(T * (T + 1) / 2);
     if (mode == 0) {
-        k_gtab_deg1<<<gt, 128, 0, st>>>(nt, (const QPoint*)qp, k, G);
+        k_gtab_sym<0><<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, geo, k, G);
     } else if (mode == 1) {
         k_gtab_moments<<<gt, 128, 0, st>>>(nt, geo, qp, nq, k, G);
     } else {
-        k_gtab_approx<<<gt, 128, 0, st>>>(nt, geo, k, G);
+        k_gtab_sym<1><<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, geo, k, G);
     }
     if (mode != 2)
         k_split_moments<<<unsigned((4 * n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, qps, nq, k,

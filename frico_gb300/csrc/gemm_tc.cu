@@ -1,0 +1,407 @@
+// Tensor-core (tcgen05) trailing update of the complex64 LU: C -= A B.
+//
+// Complex interleaved storage maps onto one real GEMM. With A (m x k) and
+// B (k x n) complex, column-major:
+//   A* (2m x 2k, K-major):  row 2r   = (Ar[r,0], -Ai[r,0], Ar[r,1], -Ai[r,1], ...)
+//                           row 2r+1 = (Ai[r,0],  Ar[r,0], Ai[r,1],  Ar[r,1], ...)
+//   B^ (n x 2k, K-major):   row j    = (Br[0,j], Bi[0,j], Br[1,j], Bi[1,j], ...)
+//                                      = column j of B as it lies in memory
+//   (A* B^T)[2r + s, j] = Re/Im (A B)[r, j]  for s = 0/1,
+// i.e. the real product lands exactly in the interleaved column-major layout
+// of C, which the epilogue updates in place.
+//
+// Precision: 3xTF32. Every operand x is split into hi = x with the low 13
+// mantissa bits cleared (exactly what the TF32 datapath reads) and
+// lo = x - hi; the MMA chain accumulates hi*hi + hi*lo + lo*hi in FP32, which
+// keeps the update at FP32-level accuracy.
+//
+// Kernel: persistent, warp-specialised, one CTA per SM.
+//   warp 0      TMA producer: per 32-float K slab, the four 128 x 32 operand
+//               tiles (A hi/lo, B hi/lo) into a 3-stage shared-memory ring,
+//               128-byte swizzle.
+//   warp 1      allocates 256 TMEM columns (two 128 x 128 FP32 accumulators)
+//               and issues tcgen05.mma (M = 128, N = 128, K = 8 per
+//               instruction); tcgen05.commit frees ring stages and publishes
+//               finished accumulators.
+//   warps 2..5  epilogue: tcgen05.ld of the accumulator (each warp its
+//               32-lane quadrant), C -= D with coalesced column loads/stores.
+// All mbarrier waits are bounded; on timeout the CTA records
+// FRICO_DEV_ERR_TIMEOUT in the status word and leaves its loops.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace frico {
+
+namespace tc {
+
+static const int BM = 128, BN = 128, BK = 32;    // tile rows, tile cols, floats per K slab (128 B)
+static const int STAGES = 3;
+static const int TILE_BYTES = BM * BK * 4;       // 16 KB (A and B tiles are both 128 x 32 floats)
+static const int STAGE_BYTES = 4 * TILE_BYTES;   // A hi, A lo, B hi, B lo
+static const int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+static const int TMEM_COLS = 256;
+static const long long kWait = 4000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on timeout / abort.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, DeviceStatus* st) {
+    const uint32_t a = smem_u32(bar);
+    long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kWait) {
+            atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT);
+            return false;
+        }
+        if (*(volatile int*)&st->err) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
+// 8-row core-matrix groups 1024 B apart (SBO), start address in 16-byte units.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= uint64_t((saddr & 0x3FFFF) >> 4);          // bits  0-13 start address
+    d |= uint64_t(1) << 16;                          // bits 16-29 leading byte offset (unused with swizzle)
+    d |= uint64_t(1024 >> 4) << 32;                  // bits 32-45 stride byte offset
+    d |= uint64_t(1) << 46;                          // bits 46-48 fixed 0b001
+    d |= uint64_t(2) << 61;                          // bits 61-63 swizzle mode: 128B
+    return d;
+}
+
+// Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major,
+// N = 128, M = 128.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+struct GemmArgs {
+    float* C;          // real view of the complex C: M x N column-major, ld = ldc floats
+    int64_t ldc;
+    int M, N, KP;      // KP = padded K in floats (multiple of 32)
+    DeviceStatus* st;
+};
+
+__global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ CUtensorMap tmAh,
+                                                        const __grid_constant__ CUtensorMap tmAl,
+                                                        const __grid_constant__ CUtensorMap tmBh,
+                                                        const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    // 1024-byte aligned ring (128-byte swizzle atoms repeat every 1024 B)
+    unsigned char* ring = (unsigned char*)((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
+    uint64_t* bars = (uint64_t*)(ring + STAGES * STAGE_BYTES);
+    uint64_t* full = bars;                 // [STAGES]
+    uint64_t* empty = bars + STAGES;       // [STAGES]
+    uint64_t* tfull = bars + 2 * STAGES;   // [2]
+    uint64_t* tempty = bars + 2 * STAGES + 2;  // [2]
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 4);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_m = (g.M + BM - 1) / BM, tiles_n = (g.N + BN - 1) / BN;
+    const int ntiles = tiles_m * tiles_n;
+    const int kslabs = g.KP / BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 4);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int mt = t % tiles_m, nt_ = t / tiles_m;
+                for (int ks = 0; ks < kslabs; ks++, it++) {
+                    const int s = it % STAGES, round = it / STAGES;
+                    if (!(ok = mbar_wait(&empty[s], (round & 1) ^ 1, g.st))) break;
+                    unsigned char* base = ring + s * STAGE_BYTES;
+                    mbar_expect_tx(&full[s], STAGE_BYTES);
+                    tma_load_2d(base, &tmAh, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + TILE_BYTES, &tmAl, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + 2 * TILE_BYTES, &tmBh, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base + 3 * TILE_BYTES, &tmBl, &full[s], ks * BK, nt_ * BN);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(BM, BN);
+            int it = 0, tcount = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, tcount++) {
+                const int acc = tcount & 1, around = tcount >> 1;
+                if (!(ok = mbar_wait(&tempty[acc], (around & 1) ^ 1, g.st))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t tmem_d = tmem_base + uint32_t(acc * BN);
+                for (int ks = 0; ks < kslabs; ks++, it++) {
+                    const int s = it % STAGES, round = it / STAGES;
+                    if (!(ok = mbar_wait(&full[s], round & 1, g.st))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t base = smem_u32(ring + s * STAGE_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < BK / 8; kk++) {
+                        const uint32_t off = uint32_t(kk * 32);   // 8 TF32 = 32 bytes along K
+                        const uint64_t ah = smem_desc_sw128(base + off);
+                        const uint64_t al = smem_desc_sw128(base + TILE_BYTES + off);
+                        const uint64_t bh = smem_desc_sw128(base + 2 * TILE_BYTES + off);
+                        const uint64_t bl = smem_desc_sw128(base + 3 * TILE_BYTES + off);
+                        const uint32_t first = (ks == 0 && kk == 0) ? 0u : 1u;
+                        mma_tf32(tmem_d, ah, bh, idesc, first);
+                        mma_tf32(tmem_d, ah, bl, idesc, 1u);
+                        mma_tf32(tmem_d, al, bh, idesc, 1u);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                mma_commit(&tfull[acc]);
+            }
+        }
+    } else {
+        // epilogue warps 2..5: TMEM lane quadrant = warp % 4
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        int tcount = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, tcount++) {
+            const int acc = tcount & 1, around = tcount >> 1;
+            const int mt = t % tiles_m, nt_ = t / tiles_m;
+            if (!mbar_wait(&tfull[acc], around & 1, g.st)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int gr = mt * BM + row;
+            const uint32_t taddr = tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * BN);
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32];
+                tmem_ld32(taddr + uint32_t(c0), v);
+                if (gr < g.M) {
+                    float* cp = g.C + int64_t(nt_ * BN + c0) * g.ldc + gr;
+                    const int ncol = min(32, g.N - (nt_ * BN + c0));
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        if (j < ncol) cp[int64_t(j) * g.ldc] -= v[j];
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[acc]);
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS));
+    }
+}
+
+// A* hi/lo from the complex panel L (m x k, column-major, lda): rows 2r, 2r+1,
+// KP floats each (zero beyond 2k). A CTA handles 32 complex rows.
+__global__ void __launch_bounds__(256) k_split_a(const float2* __restrict__ L, int64_t lda, int m, int k, int KP,
+                                                float* __restrict__ Ah, float* __restrict__ Al) {
+    __shared__ float2 t[32][65];
+    const int r0 = blockIdx.x * 32;
+    for (int q0 = 0; q0 < KP / 2; q0 += 64) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
+            int rr = idx & 31, qq = idx >> 5;
+            int r = r0 + rr, q = q0 + qq;
+            t[rr][qq] = (r < m && q < k) ? L[int64_t(q) * lda + r] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        // 64 real rows x 128 floats of this chunk
+        for (int idx = threadIdx.x; idx < 64 * 128; idx += blockDim.x) {
+            int col = idx & 127, rrow = idx >> 7;   // rrow = 2*rr + s
+            int rr = rrow >> 1, s = rrow & 1, qq = col >> 1, part = col & 1;
+            int r = r0 + rr;
+            if (r >= m || q0 + qq >= KP / 2) continue;
+            float2 a = t[rr][qq];
+            float x = s == 0 ? (part == 0 ? a.x : -a.y) : (part == 0 ? a.y : a.x);
+            float hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+            int64_t o = int64_t(2 * r + s) * KP + 2 * q0 + col;
+            Ah[o] = hi;
+            Al[o] = x - hi;
+        }
+    }
+}
+
+// B^ hi/lo from the complex block U (k x n, column-major, lda): row j = the
+// 2k floats of column j, zero-padded to KP.
+__global__ void k_split_b(const float2* __restrict__ U, int64_t lda, int k, int n, int KP, float* __restrict__ Bh,
+                          float* __restrict__ Bl) {
+    int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (idx >= int64_t(n) * KP) return;
+    int j = int(idx / KP), c = int(idx % KP);
+    float x = 0.f;
+    if (c < 2 * k) {
+        const float* col = (const float*)(U + int64_t(j) * lda);
+        x = col[c];
+    }
+    float hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    Bh[idx] = hi;
+    Bl[idx] = x - hi;
+}
+
+}  // namespace tc
+
+// ------------------------------------------------------------------ host side
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// rows x KP floats, row-major (K-major), box 128 rows x 32 floats, 128B swizzle.
+static bool make_map(CUtensorMap* m, float* base, int rows, int KP) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {cuuint64_t(KP), cuuint64_t(rows)};
+    cuuint64_t strides[1] = {cuuint64_t(KP) * 4};
+    cuuint32_t box[2] = {uint32_t(tc::BK), uint32_t(tc::BM)};
+    cuuint32_t es[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+bool gemm_tc_available(frico_gpu_ctx* ctx) {
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, ctx->device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, ctx->device);
+    return major == 10 && minor == 3 && encode_fn() != nullptr;
+}
+
+// C[m x n] -= L[m x k] * U[k x n], complex64 column-major, leading dims ldc, ldl, ldu.
+int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl, const float2* U,
+                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev) {
+    if (m <= 0 || n <= 0 || k <= 0) return FRICO_GPU_OK;
+    const int KP = ((2 * k + tc::BK - 1) / tc::BK) * tc::BK;
+    const int M = 2 * m;
+    const size_t a_elems = size_t(M) * KP, b_elems = size_t(n) * KP;
+    int rc;
+    if ((rc = ensure(ctx, ctx->tc_ws, sizeof(float) * 2 * (a_elems + b_elems) + 4096))) return rc;
+    float* Ah = (float*)(((uintptr_t)ctx->tc_ws.p + 1023) & ~uintptr_t(1023));
+    float* Al = Ah + a_elems;
+    float* Bh = Al + a_elems;
+    float* Bl = Bh + b_elems;
+    cudaStream_t st = ctx->stream;
+    tc::k_split_a<<<(m + 31) / 32, 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al);
+    tc::k_split_b<<<unsigned((b_elems + 255) / 256), 256, 0, st>>>(U, ldu, k, n, KP, Bh, Bl);
+    count_launch(ctx, 2);
+    CUtensorMap mah, mal, mbh, mbl;
+    if (!make_map(&mah, Ah, M, KP) || !make_map(&mal, Al, M, KP) || !make_map(&mbh, Bh, n, KP) ||
+        !make_map(&mbl, Bl, n, KP))
+        return set_err(ctx, FRICO_GPU_ECUDA, "cuTensorMapEncodeTiled failed");
+    static bool attr_set = false;
+    if (!attr_set) {
+        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(tc::k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      tc::SMEM_BYTES), "tc smem attribute")))
+            return rc;
+        attr_set = true;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int ntiles = ((M + tc::BM - 1) / tc::BM) * ((n + tc::BN - 1) / tc::BN);
+    tc::GemmArgs ga;
+    ga.C = (float*)C;
+    ga.ldc = 2 * ldc;
+    ga.M = M;
+    ga.N = n;
+    ga.KP = KP;
+    ga.st = (DeviceStatus*)ctx->status.p;
+    if (ev) cudaEventRecord(ev[0], st);
+    tc::k_gemm_tf32x3<<<std::min(ntiles, sms), 192, tc::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);
+    if (ev) cudaEventRecord(ev[1], st);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");
+}
+
+}  // namespace frico

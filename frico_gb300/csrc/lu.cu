@@ -14,6 +14,7 @@
 //   trsm     U12 = L11^-1 A12 (unit lower, shared-memory forward substitution).
 //   gemm     A22 -= L21 U12, register-tiled SIMT complex GEMM.
 // Pivots are stored 1-based as LAPACK's ipiv.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -203,6 +204,138 @@ __global__ void __launch_bounds__(256) k_panel(cplx<R>* A, int64_t lda, int n, i
     }
 }
 
+// Panel leaf on one thread-block cluster (<= 16 CTAs). The rows [k0, n) of
+// columns [k0, k0+jb) are split across the cluster's CTAs and stay in shared
+// memory for the whole leaf. Per column: each CTA publishes its pivot
+// candidate (value, row, the row itself) and, if it owns row k, row k in its
+// own shared memory (two parity slots); one hardware cluster barrier; then
+// every CTA reads the candidates of all CTAs through distributed shared
+// memory, picks the pivot (max |re|+|im|, lowest row on ties, as izamax),
+// swaps, scales and applies the rank-1 update to its rows. Parity slots make
+// one barrier per column sufficient: slot c&1 is rewritten only at column c+2,
+// after every CTA has passed barrier c+1.
+template <typename R>
+__global__ void __launch_bounds__(256) k_panel_cluster(cplx<R>* A, int64_t lda, int n, int k0, int jb, int rows_per,
+                                                      int32_t* ipiv, DeviceStatus* st) {
+    using C = cplx<R>;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C* sm = (C*)smraw;                         // [jb][rows_per]
+    C* cdata = sm + size_t(jb) * rows_per;     // [2][jb] candidate row
+    C* kdata = cdata + 2 * jb;                 // [2][jb] row k (owner only)
+    C* prow = kdata + 2 * jb;                  // [jb] pivot row (local copy)
+    C* krow = prow + jb;                       // [jb] old row k (local copy)
+    __shared__ R cval[2];
+    __shared__ int crow[2];
+    __shared__ R s_val;
+    __shared__ int s_row, s_p, s_g;
+    const int g = int(cluster.block_rank()), tid = threadIdx.x, G = int(cluster.num_blocks());
+    const int r0 = k0 + g * rows_per;
+    const int nr = max(0, min(n, r0 + rows_per) - r0);
+
+    for (int idx = tid; idx < nr * jb; idx += blockDim.x) {
+        int r = idx % nr, c = idx / nr;
+        sm[c * rows_per + r] = A[int64_t(k0 + c) * lda + r0 + r];
+    }
+    __syncthreads();
+
+    auto publish = [&](int c, int par) {
+        const int k = k0 + c;
+        block_argmax<R>(sm + c * rows_per, max(0, k - r0), nr, &s_val, &s_row);
+        if (tid == 0) {
+            cval[par] = s_val;
+            crow[par] = s_val >= R(0) ? r0 + s_row : 0x7fffffff;
+        }
+        if (s_val >= R(0))
+            for (int cc = tid; cc < jb; cc += blockDim.x) cdata[par * jb + cc] = sm[cc * rows_per + s_row];
+        if (k >= r0 && k < r0 + nr)
+            for (int cc = tid; cc < jb; cc += blockDim.x) kdata[par * jb + cc] = sm[cc * rows_per + (k - r0)];
+    };
+
+    publish(0, 0);
+    for (int c = 0; c < jb; c++) {
+        const int k = k0 + c, par = c & 1;
+        cluster.sync();
+        if (tid < 32) {
+            R bv = R(-1);
+            int brow = 0x7fffffff, bg = 0;
+            if (tid < G) {
+                R* rv = cluster.map_shared_rank(cval, tid);
+                int* rr = cluster.map_shared_rank(crow, tid);
+                bv = rv[par];
+                brow = rr[par];
+                bg = tid;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                R ov = __shfl_down_sync(0xffffffffu, bv, o);
+                int orr = __shfl_down_sync(0xffffffffu, brow, o);
+                int og = __shfl_down_sync(0xffffffffu, bg, o);
+                if (ov > bv || (ov == bv && orr < brow)) { bv = ov; brow = orr; bg = og; }
+            }
+            if (tid == 0) { s_p = brow; s_g = bg; }
+        }
+        __syncthreads();
+        const int p = s_p, wg = s_g;
+        const int kown = (k - k0) / rows_per;
+        {
+            const C* rc = cluster.map_shared_rank(cdata, wg) + par * jb;
+            const C* rk = cluster.map_shared_rank(kdata, kown) + par * jb;
+            for (int cc = tid; cc < jb; cc += blockDim.x) {
+                prow[cc] = rc[cc];
+                krow[cc] = rk[cc];
+            }
+        }
+        __syncthreads();
+        if (k >= r0 && k < r0 + nr)
+            for (int cc = tid; cc < jb; cc += blockDim.x) sm[cc * rows_per + (k - r0)] = prow[cc];
+        if (p != k && p >= r0 && p < r0 + nr)
+            for (int cc = tid; cc < jb; cc += blockDim.x) sm[cc * rows_per + (p - r0)] = krow[cc];
+        if (g == 0 && tid == 0) ipiv[k] = p + 1;
+        __syncthreads();
+        C piv = prow[c];
+        C inv;
+        if (piv.x == R(0) && piv.y == R(0)) {
+            inv = cmake(R(0), R(0));
+            if (g == 0 && tid == 0) atomicCAS(&st->info, 0, k + 1);
+        } else {
+            inv = cdiv(cmake(R(1), R(0)), piv);
+        }
+        const int rs = max(0, k + 1 - r0);
+        for (int r = rs + tid; r < nr; r += blockDim.x) sm[c * rows_per + r] = cmul(sm[c * rows_per + r], inv);
+        __syncthreads();
+        const int nrr = nr - rs, ncols = jb - c - 1;
+        if (nrr > 0)
+            for (int idx = tid; idx < nrr * ncols; idx += blockDim.x) {
+                int r = rs + idx % nrr, cc = c + 1 + idx / nrr;
+                sm[cc * rows_per + r] = cfms(sm[cc * rows_per + r], sm[c * rows_per + r], prow[cc]);
+            }
+        __syncthreads();
+        if (c + 1 < jb) publish(c + 1, par ^ 1);
+    }
+    for (int idx = tid; idx < nr * jb; idx += blockDim.x) {
+        int r = idx % nr, c = idx / nr;
+        A[int64_t(k0 + c) * lda + r0 + r] = sm[c * rows_per + r];
+    }
+    cluster.sync();   // no CTA leaves while others may still read its shared memory
+}
+
+// Row interchanges k <-> ipiv[k]-1 for k in [p0, p1), applied to columns [c0, c1).
+template <typename C>
+__global__ void k_laswp_range(C* A, int64_t lda, int c0, int c1, int p0, int p1, const int32_t* ipiv) {
+    int col = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= c1) return;
+    C* a = A + int64_t(col) * lda;
+    for (int k = p0; k < p1; k++) {
+        int p = ipiv[k] - 1;
+        if (p != k) {
+            C x = a[k];
+            a[k] = a[p];
+            a[p] = x;
+        }
+    }
+}
+
 // Row interchanges k <-> ipiv[k]-1, k in [k0, k0+jb), on the columns outside
 // the panel (LAPACK zlaswp applied left and right).
 template <typename C>
@@ -223,33 +356,35 @@ __global__ void k_laswp(C* A, int64_t lda, int n, int k0, int jb, const int32_t*
 }
 
 // U12 = L11^{-1} A12; a CTA owns 32 columns, 8 row groups of 32 threads.
+// B is stored row-major with the 32 columns contiguous, so the 32 lanes of a
+// warp (one column each) touch 32 consecutive words; L reads are broadcasts.
 template <typename C>
-__global__ void __launch_bounds__(256) k_trsm_lower_unit(C* A, int64_t lda, int n, int k0, int jb) {
+__global__ void __launch_bounds__(256) k_trsm_lower_unit(C* A, int64_t lda, int k0, int jb, int cb, int ce) {
     extern __shared__ __align__(16) unsigned char smraw[];
     C* L = (C*)smraw;           // [jb][jb] column-major
-    C* B = L + jb * jb;         // [32][jb] column-major per column
-    const int c0 = k0 + jb + blockIdx.x * 32;
-    const int nc = min(32, n - c0);
+    C* B = L + jb * jb;         // [jb rows][32 cols]
+    const int c0 = cb + blockIdx.x * 32;
+    const int nc = min(32, ce - c0);
     for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
         int r = idx % jb, c = idx / jb;
         L[idx] = A[int64_t(k0 + c) * lda + k0 + r];
     }
     for (int idx = threadIdx.x; idx < jb * nc; idx += blockDim.x) {
         int r = idx % jb, c = idx / jb;
-        B[c * jb + r] = A[int64_t(c0 + c) * lda + k0 + r];
+        B[r * 32 + c] = A[int64_t(c0 + c) * lda + k0 + r];
     }
     __syncthreads();
     const int lc = threadIdx.x & 31, rg = threadIdx.x >> 5;
     for (int q = 0; q < jb; q++) {
         if (lc < nc) {
-            C xq = B[lc * jb + q];
-            for (int r = q + 1 + rg; r < jb; r += 8) B[lc * jb + r] = cfms(B[lc * jb + r], L[q * jb + r], xq);
+            C xq = B[q * 32 + lc];
+            for (int r = q + 1 + rg; r < jb; r += 8) B[r * 32 + lc] = cfms(B[r * 32 + lc], L[q * jb + r], xq);
         }
         __syncthreads();
     }
     for (int idx = threadIdx.x; idx < jb * nc; idx += blockDim.x) {
         int r = idx % jb, c = idx / jb;
-        A[int64_t(c0 + c) * lda + k0 + r] = B[c * jb + r];
+        A[int64_t(c0 + c) * lda + k0 + r] = B[r * 32 + c];
     }
 }
 
@@ -257,8 +392,8 @@ __global__ void __launch_bounds__(256) k_trsm_lower_unit(C* A, int64_t lda, int 
 // 64x64 CTA tile, 16 k-slab, 256 threads, each thread 4x4 complex outputs
 // (rows tx + 16*i, cols ty + 16*j: conflict-free shared-memory reads).
 template <typename R>
-__global__ void __launch_bounds__(256) k_gemm_update(cplx<R>* Cm, const cplx<R>* Am, const cplx<R>* Bm,
-                                                     int64_t lda, int m, int nn, int kk) {
+__global__ void __launch_bounds__(256) k_gemm_update(cplx<R>* Cm, int64_t ldc, const cplx<R>* Am, int64_t lda,
+                                                     const cplx<R>* Bm, int64_t ldb, int m, int nn, int kk) {
     using C = cplx<R>;
     __shared__ C As[16][64];
     __shared__ C Bs[16][64];
@@ -276,7 +411,7 @@ __global__ void __launch_bounds__(256) k_gemm_update(cplx<R>* Cm, const cplx<R>*
             As[c][r] = (gr < m && gc < kk) ? Am[int64_t(gc) * lda + gr] : cmake(R(0), R(0));
             int br = idx & 15, bc = idx >> 4;  // B tile: 16 rows x 64 cols
             int gbr = k0 + br, gbc = bn + bc;
-            Bs[br][bc] = (gbr < kk && gbc < nn) ? Bm[int64_t(gbc) * lda + gbr] : cmake(R(0), R(0));
+            Bs[br][bc] = (gbr < kk && gbc < nn) ? Bm[int64_t(gbc) * ldb + gbr] : cmake(R(0), R(0));
         }
         __syncthreads();
 #pragma unroll
@@ -302,7 +437,7 @@ __global__ void __launch_bounds__(256) k_gemm_update(cplx<R>* Cm, const cplx<R>*
         for (int j = 0; j < 4; j++) {
             int gr = bm + tx + 16 * i, gc = bn + ty + 16 * j;
             if (gr < m && gc < nn) {
-                C* p = Cm + int64_t(gc) * lda + gr;
+                C* p = Cm + int64_t(gc) * ldc + gr;
                 *p = csub(*p, acc[i][j]);
             }
         }
@@ -336,139 +471,71 @@ __global__ void k_gather_rows(int n, int nrhs, const int32_t* perm, const CI* B,
     W[c * ldw + r] = {decltype(W[0].x)(v.x), decltype(W[0].x)(v.y)};
 }
 
-static const int kTB = 64;   // triangular-solve block
-static const int kTR = 8;    // RHS columns per pass
+static const int kTR = 8;    // RHS columns per residual pass
 
-// Forward substitution with the unit lower factor, block rows [kb, kb+nb):
-// every CTA solves the diagonal block in shared memory, CTA 0 stores it, and
-// each CTA then updates 256 rows below the block.
-template <typename C>
-__global__ void __launch_bounds__(256) k_trsv_lower(const C* LU, int64_t lda, int n, int kb, int nb,
-                                                   C* W, int64_t ldw, int nrhs) {
-    __shared__ C Ld[kTB * kTB];
-    __shared__ C X[kTB * kTR];
-    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-        int r = idx % nb, c = idx / nb;
-        Ld[c * kTB + r] = LU[int64_t(kb + c) * lda + kb + r];
-    }
-    const int r = kb + nb + blockIdx.x * blockDim.x + threadIdx.x;
-    for (int c0 = 0; c0 < nrhs; c0 += kTR) {
-        const int nc = min(kTR, nrhs - c0);
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
-            int rr = idx % nb, c = idx / nb;
-            X[c * kTB + rr] = W[int64_t(c0 + c) * ldw + kb + rr];
-        }
-        __syncthreads();
-        for (int q = 0; q < nb; q++) {
-            int cnt = (nb - q - 1) * nc;
-            for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-                int rr = q + 1 + idx % (nb - q - 1), c = idx / (nb - q - 1);
-                X[c * kTB + rr] = cfms(X[c * kTB + rr], Ld[q * kTB + rr], X[c * kTB + q]);
-            }
-            __syncthreads();
-        }
-        if (blockIdx.x == 0)
-            for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
-                int rr = idx % nb, c = idx / nb;
-                W[int64_t(c0 + c) * ldw + kb + rr] = X[c * kTB + rr];
-            }
-        if (r < n) {
-            C acc[kTR];
-            for (int c = 0; c < nc; c++) acc[c] = W[int64_t(c0 + c) * ldw + r];
-            for (int q = 0; q < nb; q++) {
-                C l = LU[int64_t(kb + q) * lda + r];
-                for (int c = 0; c < nc; c++) acc[c] = cfms(acc[c], l, X[c * kTB + q]);
-            }
-            for (int c = 0; c < nc; c++) W[int64_t(c0 + c) * ldw + r] = acc[c];
-        }
-    }
-}
-
-// Back substitution with the upper factor for block rows [kb, kb+nb), then the
-// rows above the block.
-template <typename C>
-__global__ void __launch_bounds__(256) k_trsv_upper(const C* LU, int64_t lda, int n, int kb, int nb,
-                                                   C* W, int64_t ldw, int nrhs) {
-    __shared__ C Ud[kTB * kTB];
-    __shared__ C X[kTB * kTR];
-    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-        int r = idx % nb, c = idx / nb;
-        Ud[c * kTB + r] = LU[int64_t(kb + c) * lda + kb + r];
-    }
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;  // rows above kb
-    for (int c0 = 0; c0 < nrhs; c0 += kTR) {
-        const int nc = min(kTR, nrhs - c0);
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
-            int rr = idx % nb, c = idx / nb;
-            X[c * kTB + rr] = W[int64_t(c0 + c) * ldw + kb + rr];
-        }
-        __syncthreads();
-        for (int q = nb - 1; q >= 0; q--) {
-            if (threadIdx.x < nc) {
-                int c = threadIdx.x;
-                X[c * kTB + q] = cdiv(X[c * kTB + q], Ud[q * kTB + q]);
-            }
-            __syncthreads();
-            int cnt = q * nc;
-            for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-                int rr = idx % q, c = idx / q;
-                X[c * kTB + rr] = cfms(X[c * kTB + rr], Ud[q * kTB + rr], X[c * kTB + q]);
-            }
-            __syncthreads();
-        }
-        if (blockIdx.x == 0)
-            for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
-                int rr = idx % nb, c = idx / nb;
-                W[int64_t(c0 + c) * ldw + kb + rr] = X[c * kTB + rr];
-            }
-        if (r < kb) {
-            C acc[kTR];
-            for (int c = 0; c < nc; c++) acc[c] = W[int64_t(c0 + c) * ldw + r];
-            for (int q = 0; q < nb; q++) {
-                C u = LU[int64_t(kb + q) * lda + r];
-                for (int c = 0; c < nc; c++) acc[c] = cfms(acc[c], u, X[c * kTB + q]);
-            }
-            for (int c = 0; c < nc; c++) W[int64_t(c0 + c) * ldw + r] = acc[c];
-        }
-    }
-}
-
-// R = B - Z X in FP64 (refinement residual), one thread per row, X staged in
-// shared memory 128 columns at a time.
-__global__ void __launch_bounds__(256) k_residual(const double2* Z, int64_t ldz, int n, const double2* X,
-                                                 const double2* B, double2* Rr, int64_t ld, int nrhs) {
+// Partial products of the FP64 refinement residual. The FP64 pipe is narrow on
+// this part, so the work is spread over rows (256 per CTA) and over column
+// chunks (blockIdx.y): part[(y * nrhs + c) * n + r] = sum_{i in chunk y} Z[r, i] X[i, c].
+__global__ void __launch_bounds__(256) k_residual_part(const double2* __restrict__ Z, int64_t ldz, int n,
+                                                      const double2* __restrict__ X, int64_t ld, int nrhs,
+                                                      int chunk, double2* __restrict__ part) {
     __shared__ double2 xs[128 * kTR];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
     for (int c0 = 0; c0 < nrhs; c0 += kTR) {
         const int nc = min(kTR, nrhs - c0);
         double2 acc[kTR];
+#pragma unroll
         for (int c = 0; c < kTR; c++) acc[c] = make_double2(0, 0);
-        for (int i0 = 0; i0 < n; i0 += 128) {
-            const int ni = min(128, n - i0);
+        for (int i0 = j0; i0 < j1; i0 += 128) {
+            const int ni = min(128, j1 - i0);
             __syncthreads();
             for (int idx = threadIdx.x; idx < ni * nc; idx += blockDim.x) {
                 int ii = idx % ni, c = idx / ni;
                 xs[c * 128 + ii] = X[int64_t(c0 + c) * ld + i0 + ii];
             }
             __syncthreads();
-            if (r < n)
-                for (int ii = 0; ii < ni; ii++) {
-                    double2 z = Z[int64_t(i0 + ii) * ldz + r];
-                    for (int c = 0; c < nc; c++) {
-                        double2 x = xs[c * 128 + ii];
-                        acc[c].x += z.x * x.x - z.y * x.y;
-                        acc[c].y += z.x * x.y + z.y * x.x;
+            if (r < n) {
+                const double2* zp = Z + int64_t(i0) * ldz + r;
+                if (nc == 1) {
+#pragma unroll 8
+                    for (int ii = 0; ii < ni; ii++) {
+                        double2 z = zp[int64_t(ii) * ldz];
+                        double2 x = xs[ii];
+                        acc[0].x += z.x * x.x - z.y * x.y;
+                        acc[0].y += z.x * x.y + z.y * x.x;
+                    }
+                } else {
+                    for (int ii = 0; ii < ni; ii++) {
+                        double2 z = zp[int64_t(ii) * ldz];
+#pragma unroll
+                        for (int c = 0; c < kTR; c++)
+                            if (c < nc) {
+                                double2 x = xs[c * 128 + ii];
+                                acc[c].x += z.x * x.x - z.y * x.y;
+                                acc[c].y += z.x * x.y + z.y * x.x;
+                            }
                     }
                 }
+            }
         }
         if (r < n)
-            for (int c = 0; c < nc; c++) {
-                double2 b = B[int64_t(c0 + c) * ld + r];
-                Rr[int64_t(c0 + c) * ld + r] = make_double2(b.x - acc[c].x, b.y - acc[c].y);
-            }
+#pragma unroll
+            for (int c = 0; c < kTR; c++)
+                if (c < nc) part[(int64_t(blockIdx.y) * nrhs + c0 + c) * n + r] = acc[c];
     }
+}
+
+// R = B - sum over chunks of the partial products (fixed chunk order).
+__global__ void k_residual_reduce(int n, int nrhs, int nchunks, const double2* __restrict__ part,
+                                  const double2* __restrict__ B, int64_t ld, double2* __restrict__ Rr) {
+    int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (idx >= int64_t(n) * nrhs) return;
+    int r = int(idx % n), c = int(idx / n);
+    double2 acc = make_double2(0, 0);
+    for (int y = 0; y < nchunks; y++) acc = cadd(acc, part[(int64_t(y) * nrhs + c) * n + r]);
+    double2 b = B[int64_t(c) * ld + r];
+    Rr[int64_t(c) * ld + r] = make_double2(b.x - acc.x, b.y - acc.y);
 }
 
 // out[c] = sum_r |V[r,c]|^2, one CTA per column (fixed summation order).
@@ -525,6 +592,187 @@ static void prof_collect(frico_gpu_ctx* ctx) {
     ctx->prof_used = 0;
 }
 
+// Host-side launcher for one factorisation: recursive panel (zgetrf2-style
+// halving down to a leaf that fits one thread-block cluster), interchanges,
+// triangular solve and trailing GEMM.
+template <typename R> struct LuDriver {
+    using C = cplx<R>;
+    frico_gpu_ctx* ctx;
+    C* A;
+    int64_t lda;
+    int n;
+    cudaStream_t st;
+    PanelWS<R> ws;
+    DeviceStatus* dst;
+    int dev_sms = 0, coop_smem = 0, cl_smem = 0, cl_max = 8;
+    size_t trsm_smem = 0;
+    bool use_tc = false;
+
+    int init() {
+        int rc;
+        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+        cudaFuncAttributes fa;
+        if ((rc = cuda_check(ctx, cudaFuncGetAttributes(&fa, k_panel<R>), "panel attributes"))) return rc;
+        coop_smem = optin - int(fa.sharedSizeBytes);
+        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(k_panel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      coop_smem), "panel smem attribute")))
+            return rc;
+        if ((rc = cuda_check(ctx, cudaFuncGetAttributes(&fa, k_panel_cluster<R>), "cluster attributes"))) return rc;
+        cl_smem = optin - int(fa.sharedSizeBytes);
+        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(k_panel_cluster<R>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, cl_smem),
+                             "cluster smem attribute")))
+            return rc;
+        cl_max = 8;
+        if (cudaFuncSetAttribute(k_panel_cluster<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess)
+            cl_max = 16;
+        else
+            cudaGetLastError();
+        // largest cluster that can actually be placed with a full shared-memory budget
+        for (; cl_max > 1; cl_max /= 2) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(cl_max);
+            cfg.blockDim = dim3(256);
+            cfg.dynamicSmemBytes = size_t(cl_smem);
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = cl_max;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int num = 0;
+            if (cudaOccupancyMaxActiveClusters(&num, k_panel_cluster<R>, &cfg) == cudaSuccess && num > 0) break;
+            cudaGetLastError();
+        }
+        trsm_smem = sizeof(C) * (kNB * kNB + 32 * kNB);
+        const int eng = ctx->opt.gemm_engine;
+        use_tc = sizeof(R) == 4 && eng != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
+        if (eng == FRICO_GEMM_TC && sizeof(R) == 4 && !use_tc)
+            return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
+        return cuda_check(ctx, cudaFuncSetAttribute(k_trsm_lower_unit<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    int(trsm_smem)), "trsm smem attribute");
+    }
+
+    // Widest leaf (<= w, power of two >= 8) the cluster kernel can hold for m rows; 0 if none.
+    int leaf_width(int m, int w, int* cl, int* rows_per) const {
+        int CL = std::max(1, std::min(cl_max, (m + 63) / 64));
+        int rp = (m + CL - 1) / CL;
+        for (int lw = std::min(w, sizeof(R) == 4 ? 32 : 16); lw >= 8; lw /= 2) {
+            size_t smem = sizeof(C) * (size_t(rp) * lw + 6 * lw);
+            if (smem <= size_t(cl_smem)) {
+                *cl = (m + rp - 1) / rp;
+                *rows_per = rp;
+                return lw;
+            }
+        }
+        return 0;
+    }
+
+    int leaf_cluster(int k0, int w, int CL, int rows_per) {
+        size_t smem = sizeof(C) * (size_t(rows_per) * w + 6 * w);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(CL);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = CL;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int32_t* ipiv = (int32_t*)ctx->ipiv.p;
+        count_launch(ctx);
+        return cuda_check(ctx, cudaLaunchKernelEx(&cfg, k_panel_cluster<R>, A, lda, n, k0, w, rows_per, ipiv, dst),
+                          "k_panel_cluster");
+    }
+
+    int leaf_coop(int k0, int w) {
+        const int m = n - k0;
+        int G = std::max(1, std::min(dev_sms, (m + 31) / 32));
+        int rows_per = (m + G - 1) / G;
+        size_t smem = sizeof(C) * (size_t(rows_per) * w + 2 * w);
+        while (smem > size_t(coop_smem) && G < dev_sms) {
+            G++;
+            rows_per = (m + G - 1) / G;
+            smem = sizeof(C) * (size_t(rows_per) * w + 2 * w);
+        }
+        if (smem > size_t(coop_smem)) return set_err(ctx, FRICO_GPU_EINVAL, "matrix too large for panel kernel");
+        G = (m + rows_per - 1) / rows_per;
+        int maxb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_panel<R>, 256, smem);
+        if (maxb * dev_sms < G) return set_err(ctx, FRICO_GPU_ECUDA, "panel kernel cannot be co-resident");
+        int32_t* ipiv = (int32_t*)ctx->ipiv.p;
+        int64_t lda_ = lda;
+        int n_ = n, k0_ = k0, w_ = w, rp_ = rows_per;
+        PanelWS<R> ws_ = ws;
+        DeviceStatus* dst_ = dst;
+        void* args[] = {&A, &lda_, &n_, &k0_, &w_, &rp_, &ipiv, &ws_, &dst_};
+        count_launch(ctx);
+        return cuda_check(ctx, cudaLaunchCooperativeKernel((void*)k_panel<R>, dim3(G), dim3(256), args, smem, st),
+                          "k_panel");
+    }
+
+    void laswp(int c0, int c1, int p0, int p1) {
+        if (c1 <= c0 || p1 <= p0) return;
+        k_laswp_range<C><<<(c1 - c0 + 127) / 128, 128, 0, st>>>(A, lda, c0, c1, p0, p1, (const int32_t*)ctx->ipiv.p);
+        count_launch(ctx);
+    }
+
+    // A[k0:k0+w, cb:ce] <- L11^{-1} A[k0:k0+w, cb:ce], L11 unit lower at (k0, k0)
+    void trsm(int k0, int w, int cb, int ce) {
+        if (ce <= cb) return;
+        k_trsm_lower_unit<C><<<(ce - cb + 31) / 32, 256, trsm_smem, st>>>(A, lda, k0, w, cb, ce);
+        count_launch(ctx);
+    }
+
+    // A[r0:r0+m, c0:c0+nn] -= A[r0:r0+m, k0:k0+kk] * A[k0:k0+kk, c0:c0+nn]
+    int gemm(int r0, int c0, int m, int nn, int k0, int kk, bool profile) {
+        if (m <= 0 || nn <= 0) return FRICO_GPU_OK;
+        C* Cm = A + int64_t(c0) * lda + r0;
+        const C* Am = A + int64_t(k0) * lda + r0;
+        const C* Bm = A + int64_t(c0) * lda + k0;
+        dim3 gg((m + 63) / 64, (nn + 63) / 64);
+        cudaEvent_t* ev = profile ? prof_pair(ctx) : nullptr;
+        if (ev) ctx->stats.gemm_flops += 8.0 * double(m) * double(nn) * double(kk);
+        if (sizeof(R) == 4 && profile && use_tc && m >= 128 && nn >= 128) {
+            // outer trailing update on the tensor cores (events bracket the MMA kernel)
+            int rc = gemm_update_tc(ctx, (float2*)Cm, lda, (const float2*)Am, lda, (const float2*)Bm, lda, m, nn,
+                                    kk, ev);
+            if (rc) return rc;
+            return FRICO_GPU_OK;
+        }
+        if (ev) cudaEventRecord(ev[0], st);
+        k_gemm_update<R><<<gg, 256, 0, st>>>(Cm, lda, Am, lda, Bm, lda, m, nn, kk);
+        if (ev) cudaEventRecord(ev[1], st);
+        count_launch(ctx);
+        return FRICO_GPU_OK;
+    }
+
+    // Factor columns [k0, k0+w) of rows [k0, n), interchanges applied inside the panel.
+    int panel(int k0, int w) {
+        const int m = n - k0;
+        int CL = 0, rp = 0;
+        int lw = leaf_width(m, w, &CL, &rp);
+        if (lw == 0) return leaf_coop(k0, w);
+        if (w <= lw) return leaf_cluster(k0, w, CL, rp);
+        const int w1 = w / 2, w2 = w - w1;
+        int rc;
+        if ((rc = panel(k0, w1))) return rc;
+        laswp(k0 + w1, k0 + w, k0, k0 + w1);
+        trsm(k0, w1, k0 + w1, k0 + w);
+        if ((rc = gemm(k0 + w1, k0 + w1, m - w1, w2, k0, w1, false))) return rc;
+        if ((rc = panel(k0 + w1, w2))) return rc;
+        laswp(k0, k0 + w1, k0 + w1, k0 + w);
+        return FRICO_GPU_OK;
+    }
+};
+
 template <typename R>
 static int lu_factor_impl(frico_gpu_ctx* ctx, cplx<R>* A) {
     using C = cplx<R>;
@@ -550,65 +798,26 @@ static int lu_factor_impl(frico_gpu_ctx* ctx, cplx<R>* A) {
         return rc;
     DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
 
-    int dev_sms = 0, max_smem = 0;
-    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    {
-        // dynamic limit = opt-in limit minus the kernel's static shared memory
-        cudaFuncAttributes fa;
-        if ((rc = cuda_check(ctx, cudaFuncGetAttributes(&fa, k_panel<R>), "panel attributes"))) return rc;
-        max_smem -= int(fa.sharedSizeBytes);
-        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(k_panel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      max_smem), "panel smem attribute")))
-            return rc;
-    }
-    const size_t trsm_smem = sizeof(C) * (kNB * kNB + 32 * kNB);
-    cudaFuncSetAttribute(k_trsm_lower_unit<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(trsm_smem));
-
+    LuDriver<R> drv;
+    drv.ctx = ctx;
+    drv.A = A;
+    drv.lda = lda;
+    drv.n = n;
+    drv.st = st;
+    drv.ws = ws;
+    drv.dst = dst;
+    if ((rc = drv.init())) return rc;
+    int32_t* ipiv = (int32_t*)ctx->ipiv.p;
     for (int k0 = 0; k0 < n; k0 += kNB) {
         const int jb = std::min(kNB, n - k0);
-        const int m = n - k0;
-        // CTAs: at least 32 rows each, at most one per SM, shared memory bound.
-        int G = std::max(1, std::min(dev_sms, (m + 31) / 32));
-        int rows_per = (m + G - 1) / G;
-        size_t smem = sizeof(C) * (size_t(rows_per) * jb + 2 * jb);
-        while (smem > size_t(max_smem) && G < dev_sms) {
-            G++;
-            rows_per = (m + G - 1) / G;
-            smem = sizeof(C) * (size_t(rows_per) * jb + 2 * jb);
-        }
-        if (smem > size_t(max_smem)) return set_err(ctx, FRICO_GPU_EINVAL, "matrix too large for panel kernel");
-        G = (m + rows_per - 1) / rows_per;
-        int maxb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_panel<R>, 256, smem);
-        if (maxb * dev_sms < G) return set_err(ctx, FRICO_GPU_ECUDA, "panel kernel cannot be co-resident");
-        int32_t* ipiv = (int32_t*)ctx->ipiv.p;
-        int64_t lda_ = lda;
-        int n_ = n, k0_ = k0, jb_ = jb, rp_ = rows_per;
-        void* args[] = {&A, &lda_, &n_, &k0_, &jb_, &rp_, &ipiv, &ws, &dst};
-        rc = cuda_check(ctx, cudaLaunchCooperativeKernel((void*)k_panel<R>, dim3(G), dim3(256), args, smem, st),
-                        "k_panel");
-        if (rc) return rc;
-        count_launch(ctx);
-        if (n - jb > 0) {
-            k_laswp<C><<<(n - jb + 255) / 256, 256, 0, st>>>(A, lda, n, k0, jb, ipiv);
-            count_launch(ctx);
-        }
+        if ((rc = drv.panel(k0, jb))) return rc;
+        // the panel's interchanges on the columns left and right of it
+        if (k0 > 0) drv.laswp(0, k0, k0, k0 + jb);
+        if (k0 + jb < n) drv.laswp(k0 + jb, n, k0, k0 + jb);
         const int rest = n - k0 - jb;
         if (rest > 0) {
-            k_trsm_lower_unit<C><<<(rest + 31) / 32, 256, trsm_smem, st>>>(A, lda, n, k0, jb);
-            C* Cm = A + int64_t(k0 + jb) * lda + k0 + jb;
-            const C* Am = A + int64_t(k0) * lda + k0 + jb;
-            const C* Bm = A + int64_t(k0 + jb) * lda + k0;
-            dim3 gg((rest + 63) / 64, (rest + 63) / 64);
-            cudaEvent_t* ev = prof_pair(ctx);
-            if (ev) cudaEventRecord(ev[0], st);
-            k_gemm_update<R><<<gg, 256, 0, st>>>(Cm, Am, Bm, lda, rest, rest, jb);
-            if (ev) {
-                cudaEventRecord(ev[1], st);
-                ctx->stats.gemm_flops += 8.0 * double(rest) * double(rest) * double(jb);
-            }
-            count_launch(ctx, 2);
+            drv.trsm(k0, jb, k0 + jb, n);
+            if ((rc = drv.gemm(k0 + jb, k0 + jb, rest, rest, k0, jb, true))) return rc;
         }
         if ((rc = cuda_check(ctx, cudaGetLastError(), "lu step"))) return rc;
     }
@@ -626,32 +835,23 @@ static int lu_factor_impl(frico_gpu_ctx* ctx, cplx<R>* A) {
         return set_err(ctx, FRICO_GPU_ETIMEOUT, buf);
     }
     ctx->info = hs.info;
-    return FRICO_GPU_OK;
+    if (hs.info != 0) return FRICO_GPU_OK;   // singular: no solve will follow
+    // clear the status word for the solves, then invert the diagonal blocks
+    if ((rc = cuda_check(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(DeviceStatus), st), "status reset")))
+        return rc;
+    return sizeof(R) == 8 ? trsv_prepare_fp64(ctx) : trsv_prepare_fp32(ctx);
 }
 
 int lu_factor_fp64(frico_gpu_ctx* ctx) { return lu_factor_impl<double>(ctx, (double2*)ctx->z64.p); }
 int lu_factor_fp32(frico_gpu_ctx* ctx) { return lu_factor_impl<float>(ctx, (float2*)ctx->z32.p); }
 
-// Solve in place on W (already row-permuted): L then U.
-template <typename C>
-static int trsv_all(frico_gpu_ctx* ctx, const C* LU, C* W, int nrhs, int64_t ldw) {
-    const int n = int(ctx->n);
-    cudaStream_t st = ctx->stream;
-    for (int kb = 0; kb < n; kb += kTB) {
-        int nb = std::min(kTB, n - kb);
-        int below = n - kb - nb;
-        int grid = std::max(1, (below + 255) / 256);
-        k_trsv_lower<C><<<grid, 256, 0, st>>>(LU, n, n, kb, nb, W, ldw, nrhs);
-        count_launch(ctx);
-    }
-    int last = ((n - 1) / kTB) * kTB;
-    for (int kb = last; kb >= 0; kb -= kTB) {
-        int nb = std::min(kTB, n - kb);
-        int grid = std::max(1, (kb + 255) / 256);
-        k_trsv_upper<C><<<grid, 256, 0, st>>>(LU, n, n, kb, nb, W, ldw, nrhs);
-        count_launch(ctx);
-    }
-    return cuda_check(ctx, cudaGetLastError(), "trsv");
+int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl, const float2* U,
+                       int64_t ldu, int m, int n, int k) {
+    if (m <= 0 || n <= 0) return FRICO_GPU_OK;
+    dim3 gg((m + 63) / 64, (n + 63) / 64);
+    k_gemm_update<float><<<gg, 256, 0, ctx->stream>>>(C, ldc, L, ldl, U, ldu, m, n, k);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_gemm_update");
 }
 
 // X = A^{-1} B (FP64 factors in z64), B n x nrhs (device), result into B.
@@ -664,7 +864,8 @@ int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb) {
     k_gather_rows<double2, double2><<<unsigned((cnt + 255) / 256), 256, 0, ctx->stream>>>(
         int(n), nrhs, (const int32_t*)ctx->perm.p, B, ldb, W, n);
     count_launch(ctx);
-    if ((rc = trsv_all<double2>(ctx, (const double2*)ctx->z64.p, W, nrhs, n))) return rc;
+    if ((rc = trsv_solve_fp64(ctx, W, nrhs, n))) return rc;
+    if ((rc = trsv_check(ctx))) return rc;
     for (int c = 0; c < nrhs; c++)
         if ((rc = cuda_check(ctx, cudaMemcpyAsync(B + c * ldb, W + c * n, sizeof(double2) * n,
                                                   cudaMemcpyDeviceToDevice, ctx->stream), "copy X")))
@@ -693,6 +894,15 @@ int refine_solve(frico_gpu_ctx* ctx) {
     const int max_it = ctx->opt.max_refine_iters > 0 ? ctx->opt.max_refine_iters : 30;
     const double tol = ctx->opt.refine_tol > 0 ? ctx->opt.refine_tol : 1e-12;
     std::vector<double> hn(2 * nrhs);
+    // residual split: 256 rows x `chunk` columns per CTA, ~4 CTAs per SM
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const unsigned rblocks = unsigned((n + 255) / 256);
+    int nchunks = std::max(1, std::min(int(n / 128), int((4 * sms + rblocks - 1) / rblocks)));
+    const int chunk = int((n + nchunks - 1) / nchunks);
+    nchunks = int((n + chunk - 1) / chunk);
+    if ((rc = ensure(ctx, ctx->rwork32, sizeof(double2) * size_t(nchunks) * nrhs * n))) return rc;
+    double2* part = (double2*)ctx->rwork32.p;
     k_colnorm2<double2><<<nrhs, 256, 0, st>>>(int(n), B, n, nrm + nrhs);
     count_launch(ctx);
     const double2* src = B;
@@ -701,16 +911,18 @@ int refine_solve(frico_gpu_ctx* ctx) {
     for (; it < max_it; it++) {
         k_gather_rows<double2, float2><<<unsigned((cnt + 255) / 256), 256, 0, st>>>(
             int(n), nrhs, (const int32_t*)ctx->perm.p, src, n, W, n);
-        if ((rc = trsv_all<float2>(ctx, LU, W, nrhs, n))) return rc;
+        if ((rc = trsv_solve_fp32(ctx, W, nrhs, n))) return rc;
         k_add_c64_to_c128<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, W, X, it == 0);
-        k_residual<<<unsigned((n + 255) / 256), 256, 0, st>>>((const double2*)ctx->z64.p, n, int(n), X, B, Rr,
-                                                             n, nrhs);
+        k_residual_part<<<dim3(rblocks, nchunks), 256, 0, st>>>((const double2*)ctx->z64.p, n, int(n), X, n, nrhs,
+                                                               chunk, part);
+        k_residual_reduce<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(int(n), nrhs, nchunks, part, B, n, Rr);
         k_colnorm2<double2><<<nrhs, 256, 0, st>>>(int(n), Rr, n, nrm);
-        count_launch(ctx, 4);
+        count_launch(ctx, 5);
         if ((rc = cuda_check(ctx, cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs,
                                                   cudaMemcpyDeviceToHost, st), "norms")))
             return rc;
         if ((rc = cuda_check(ctx, cudaStreamSynchronize(st), "refine sync"))) return rc;
+        if ((rc = trsv_check(ctx))) return rc;
         rel = 0.0;
         for (int c = 0; c < nrhs; c++) {
             double bn = hn[nrhs + c] > 0 ? std::sqrt(hn[nrhs + c]) : 1.0;

@@ -1,0 +1,259 @@
+// Triangular solves with the LU factors (the zgetrs part of FRICO's
+// solve_general, src/lapack_wrappers.cpp:81-89), one launch per triangle.
+//
+// After factorisation the 64x64 diagonal blocks of L (unit lower) and U are
+// inverted once (k_invert_diag). A solve then runs as a single kernel whose
+// CTAs take block rows in ticket order (atomic counter, so a CTA only ever
+// waits for blocks owned by CTAs that are already running). Block row b
+// accumulates  y_b = w_b - sum_{c before b} T_bc y_c  as the y_c are published
+// (per-block flag = launch epoch), applies the inverted diagonal block and
+// publishes y_b. The only sequential part is the chain of 64-row blocks; the
+// off-diagonal work of every block overlaps with the wait. Every wait is
+// bounded: on timeout the CTA records FRICO_DEV_ERR_TIMEOUT and returns.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace frico {
+
+static const int kB = 64;        // block rows
+static const int kRc = 8;        // right-hand sides per pass
+static const long long kWaitCycles = 4000000000LL;
+
+// One CTA per diagonal block: Linv = L_bb^{-1} (unit lower), Uinv = U_bb^{-1}.
+// Thread j owns column j of the inverse (forward / backward substitution
+// against e_j); columns are held in shared memory, lanes on consecutive words.
+template <typename C>
+__global__ void __launch_bounds__(128) k_invert_diag(const C* __restrict__ LU, int64_t lda, int n, C* Linv, C* Uinv) {
+    __shared__ C T[kB][kB + 1];   // T[r][c] = block entry (row r, col c)
+    __shared__ C X[kB][kB + 1];   // X[r][j] = inverse entry (row r, col j)
+    const int b = blockIdx.x, r0 = b * kB, bs = min(kB, n - r0);
+    for (int idx = threadIdx.x; idx < kB * kB; idx += blockDim.x) {
+        int r = idx % kB, c = idx / kB;
+        T[r][c] = (r < bs && c < bs) ? LU[int64_t(r0 + c) * lda + r0 + r] : cmake(decltype(T[0][0].x)(0), decltype(T[0][0].x)(0));
+    }
+    __syncthreads();
+    using R = decltype(T[0][0].x);
+    const int j = threadIdx.x;
+    if (j < kB) {
+        // lower: X[:, j] = L^{-1} e_j
+        for (int r = 0; r < kB; r++) {
+            C s = cmake(R(r == j ? 1 : 0), R(0));
+            for (int q = j; q < r; q++) s = cfms(s, T[r][q], X[q][j]);
+            X[r][j] = (r < j) ? cmake(R(0), R(0)) : s;
+        }
+    }
+    __syncthreads();
+    C* Lo = Linv + int64_t(b) * kB * kB;
+    for (int idx = threadIdx.x; idx < kB * kB; idx += blockDim.x) {
+        int r = idx % kB, c = idx / kB;
+        Lo[idx] = X[r][c];
+    }
+    __syncthreads();
+    if (j < kB) {
+        // upper: X[:, j] = U^{-1} e_j (rows beyond bs act as identity)
+        for (int r = kB - 1; r >= 0; r--) {
+            C s = cmake(R(r == j ? 1 : 0), R(0));
+            if (r > j || r >= bs) {
+                X[r][j] = (r < bs) ? cmake(R(0), R(0)) : s;
+                continue;
+            }
+            for (int q = r + 1; q <= j && q < bs; q++) s = cfms(s, T[r][q], X[q][j]);
+            X[r][j] = cdiv(s, T[r][r]);
+        }
+    }
+    __syncthreads();
+    C* Uo = Uinv + int64_t(b) * kB * kB;
+    for (int idx = threadIdx.x; idx < kB * kB; idx += blockDim.x) {
+        int r = idx % kB, c = idx / kB;
+        Uo[idx] = X[r][c];
+    }
+}
+
+// W <- T^{-1} W for T = unit-lower L (LOWER) or upper U, nrhs <= kRc.
+template <typename C, bool LOWER>
+__global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, int64_t lda, int n, const C* __restrict__ Dinv,
+                                                   C* W, int64_t ldw, int nrhs, int* flags, unsigned* ticket, int epoch,
+                                                   DeviceStatus* st) {
+    using R = decltype(W[0].x);
+    __shared__ C xs[kB][kRc];            // a published block y_c
+    __shared__ C part[4][kB][kRc];       // partial sums of the 4 column groups
+    __shared__ int s_t;
+    const int nb = (n + kB - 1) / kB;
+    if (threadIdx.x == 0) s_t = int(atomicAdd(ticket, 1u));
+    __syncthreads();
+    const int t = s_t;
+    if (t >= nb) return;
+    const int b = LOWER ? t : nb - 1 - t;
+    const int r0 = b * kB, bs = min(kB, n - r0);
+    const int r = threadIdx.x & 63, q = threadIdx.x >> 6;   // row in block, column group (16 cols)
+    C acc[kRc];
+#pragma unroll
+    for (int c = 0; c < kRc; c++) acc[c] = cmake(R(0), R(0));
+
+    // The 16 values of T this thread needs from the next dependency block are
+    // loaded before waiting on its flag (T does not depend on the chain), so
+    // the HBM latency overlaps the wait instead of serialising per element.
+    const int ndep = LOWER ? b : nb - 1 - b;
+    C lv[16];
+    auto load_block = [&](int k) {
+        const int cb = LOWER ? k : nb - 1 - k;
+        const int c0 = cb * kB, cs = min(kB, n - c0);
+        const C* col = LU + int64_t(c0 + q * 16) * lda + r0 + r;
+#pragma unroll
+        for (int cc = 0; cc < 16; cc++)
+            lv[cc] = (r < bs && q * 16 + cc < cs) ? col[int64_t(cc) * lda] : cmake(R(0), R(0));
+    };
+    if (ndep > 0) load_block(0);
+    for (int k = 0; k < ndep; k++) {
+        const int cb = LOWER ? k : nb - 1 - k;
+        const int c0 = cb * kB, cs = min(kB, n - c0);
+        if (threadIdx.x == 0) {
+            volatile int* f = flags + cb;
+            long long t0 = clock64();
+            while (*f != epoch) {
+                if (clock64() - t0 > kWaitCycles) {
+                    if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
+                    break;
+                }
+                if (*(volatile int*)&st->err) break;
+                __nanosleep(64);
+            }
+        }
+        __syncthreads();
+        if (*(volatile int*)&st->err) return;
+        for (int idx = threadIdx.x; idx < cs * nrhs; idx += blockDim.x) {
+            int rr = idx % cs, c = idx / cs;
+            xs[rr][c] = __ldcg(&W[int64_t(c) * ldw + c0 + rr]);
+        }
+        __syncthreads();
+        C cur[16];
+#pragma unroll
+        for (int cc = 0; cc < 16; cc++) cur[cc] = lv[cc];
+        if (k + 1 < ndep) load_block(k + 1);   // prefetch the next block's T values
+        if (r < bs) {
+#pragma unroll
+            for (int cc = 0; cc < 16; cc++) {
+                if (q * 16 + cc < cs) {
+#pragma unroll
+                    for (int c = 0; c < kRc; c++)
+                        if (c < nrhs) acc[c] = cfms(acc[c], cur[cc], xs[q * 16 + cc][c]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // y_pre = w_b + sum of the four partial sums
+#pragma unroll
+    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    __syncthreads();
+    if (q == 0 && r < bs)
+        for (int c = 0; c < nrhs; c++) {
+            C s = W[int64_t(c) * ldw + r0 + r];
+            s = cadd(s, cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c])));
+            xs[r][c] = s;
+        }
+    __syncthreads();
+    // y = Dinv_b * y_pre
+    const C* D = Dinv + int64_t(b) * kB * kB;
+#pragma unroll
+    for (int c = 0; c < kRc; c++) acc[c] = cmake(R(0), R(0));
+    if (r < bs)
+        for (int cc = q * 16; cc < q * 16 + 16 && cc < bs; cc++) {
+            C d = D[cc * kB + r];
+#pragma unroll
+            for (int c = 0; c < kRc; c++)
+                if (c < nrhs) acc[c] = cadd(acc[c], cmul(d, xs[cc][c]));
+        }
+#pragma unroll
+    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    __syncthreads();
+    if (q == 0 && r < bs)
+        for (int c = 0; c < nrhs; c++)
+            W[int64_t(c) * ldw + r0 + r] = cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c]));
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicExch(flags + b, epoch);
+}
+
+// ------------------------------------------------------------------ host side
+struct TrsvWs {
+    void* dinv = nullptr;      // Linv blocks then Uinv blocks
+    int* flags = nullptr;
+    unsigned* ticket = nullptr;
+    int epoch = 0;
+};
+
+template <typename C>
+int trsv_prepare(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_buf) {
+    const int n = int(ctx->n), nb = (n + kB - 1) / kB;
+    int rc;
+    if ((rc = ensure(ctx, ws_buf, sizeof(C) * size_t(2) * nb * kB * kB))) return rc;
+    if ((rc = ensure(ctx, flag_buf, sizeof(int) * (nb + 64)))) return rc;
+    if ((rc = cuda_check(ctx, cudaMemsetAsync(flag_buf.p, 0, sizeof(int) * (nb + 64), ctx->stream), "flags")))
+        return rc;
+    C* Linv = (C*)ws_buf.p;
+    C* Uinv = Linv + size_t(nb) * kB * kB;
+    k_invert_diag<C><<<nb, 128, 0, ctx->stream>>>(LU, n, n, Linv, Uinv);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_invert_diag");
+}
+
+template <typename C>
+int trsv_solve(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_buf, C* W, int nrhs, int64_t ldw) {
+    const int n = int(ctx->n), nb = (n + kB - 1) / kB;
+    C* Linv = (C*)ws_buf.p;
+    C* Uinv = Linv + size_t(nb) * kB * kB;
+    int* flags = (int*)flag_buf.p;
+    unsigned* ticket = (unsigned*)(flags + nb + 32);
+    DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
+    int rc;
+    for (int c0 = 0; c0 < nrhs; c0 += kRc) {
+        int nc = std::min(kRc, nrhs - c0);
+        for (int pass = 0; pass < 2; pass++) {
+            int epoch = ++ctx->trsv_epoch;
+            if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream), "ticket"))) return rc;
+            if (pass == 0)
+                k_trsv_chain<C, true><<<nb, 256, 0, ctx->stream>>>(LU, n, n, Linv, W + c0 * ldw, ldw, nc, flags,
+                                                                   ticket, epoch, dst);
+            else
+                k_trsv_chain<C, false><<<nb, 256, 0, ctx->stream>>>(LU, n, n, Uinv, W + c0 * ldw, ldw, nc, flags,
+                                                                    ticket, epoch, dst);
+            count_launch(ctx);
+        }
+    }
+    return cuda_check(ctx, cudaGetLastError(), "k_trsv_chain");
+}
+
+int trsv_prepare_fp64(frico_gpu_ctx* ctx) {
+    return trsv_prepare<double2>(ctx, (const double2*)ctx->z64.p, ctx->dinv, ctx->trsv_flags);
+}
+int trsv_prepare_fp32(frico_gpu_ctx* ctx) {
+    return trsv_prepare<float2>(ctx, (const float2*)ctx->z32.p, ctx->dinv, ctx->trsv_flags);
+}
+int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw) {
+    return trsv_solve<double2>(ctx, (const double2*)ctx->z64.p, ctx->dinv, ctx->trsv_flags, W, nrhs, ldw);
+}
+int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
+    return trsv_solve<float2>(ctx, (const float2*)ctx->z32.p, ctx->dinv, ctx->trsv_flags, W, nrhs, ldw);
+}
+
+// Checks the device status word after a solve (host-synchronous).
+int trsv_check(frico_gpu_ctx* ctx) {
+    DeviceStatus hs;
+    int rc = cuda_check(ctx, cudaMemcpyAsync(&hs, ctx->status.p, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream),
+                        "status");
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    if (rc) return rc;
+    if (hs.err == FRICO_DEV_ERR_TIMEOUT) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "triangular solve wait timed out at block %d", hs.where);
+        return set_err(ctx, FRICO_GPU_ETIMEOUT, buf);
+    }
+    return FRICO_GPU_OK;
+}
+
+}  // namespace frico

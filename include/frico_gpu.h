@@ -87,8 +87,14 @@ typedef struct frico_gpu_options {
     double  refine_tol;      /* mixed precision: stop at ||r||/||b|| <= tol (<=0: 1e-12) */
     double  Z0;              /* reference impedance for gamma/SWR (-Z)       */
     int32_t profile_kernels; /* 1: CUDA-event timing of every LU update GEMM */
-    int32_t reserved;
+    int32_t gemm_engine;     /* complex64 trailing update: FRICO_GEMM_AUTO or FRICO_GEMM_SIMT */
 } frico_gpu_options;
+
+#define FRICO_GEMM_AUTO 0   /* tcgen05 3xTF32 on sm_103, SIMT otherwise */
+#define FRICO_GEMM_SIMT 1   /* CUDA-core FP32 complex GEMM               */
+#define FRICO_GEMM_TC   2   /* tcgen05 3xTF32 (error if unavailable)     */
+
+typedef struct frico_c64 { float re, im; } frico_c64;
 
 /* Port values (src/emw_ana_antenna.h:31-38). */
 typedef struct frico_port_values {
@@ -211,6 +217,13 @@ int frico_gpu_rcs_points(frico_gpu_ctx* ctx, int32_t col, double R, int64_t npts
                          const double* theta, const double* phi, double* out);
 
 int frico_gpu_last_stats(frico_gpu_ctx* ctx, frico_gpu_stats* stats);
+
+/* Diagnostic: C -= A B with the LU's complex64 trailing-update kernel
+ * (engine FRICO_GEMM_SIMT or FRICO_GEMM_TC); A m x k (ld m), B k x n (ld k),
+ * C m x n (ld m), column-major host buffers. No FRICO counterpart: it exposes
+ * one internal kernel so that it can be tested on its own. */
+int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, int32_t k, const frico_c64* A,
+                          const frico_c64* B, frico_c64* C, int32_t engine);
 
 #ifdef __cplusplus
 }
