@@ -19,6 +19,7 @@ EDGE_LENGTH_XY, EDGE_LENGTH_TRUE = 0, 1
 HPHASE_COMPAT, HPHASE_PHYSICAL = 0, 1
 GAIN_XY, GAIN_YZ, GAIN_XZ = 0, 1, 2
 GEMM_AUTO, GEMM_SIMT, GEMM_TC = 0, 1, 2
+PIVOT_AUTO, PIVOT_PARTIAL, PIVOT_NONE = 0, 1, 2
 
 # numpy mirror of frico_rwg (112 bytes)
 RWG_DTYPE = np.dtype([
@@ -37,7 +38,7 @@ class Options(C.Structure):
     _fields_ = [("degree", C.c_int32), ("approx", C.c_int32), ("force_symmetry", C.c_int32),
                 ("precision", C.c_int32), ("h_phase_mode", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("refine_tol", C.c_double), ("Z0", C.c_double), ("profile_kernels", C.c_int32),
-                ("gemm_engine", C.c_int32)]
+                ("gemm_engine", C.c_int32), ("pivoting", C.c_int32), ("reserved", C.c_int32)]
 
 
 class PortValues(C.Structure):
@@ -51,7 +52,7 @@ class Stats(C.Structure):
                 ("fields_ms", C.c_double), ("refine_iters", C.c_int32), ("refine_residual", C.c_double),
                 ("n", C.c_int64), ("ntri", C.c_int64), ("nrhs", C.c_int64), ("green_evals", C.c_int64),
                 ("kernel_launches", C.c_int64), ("gemm_launches", C.c_int64), ("gemm_ms", C.c_double),
-                ("gemm_flops", C.c_double)]
+                ("gemm_flops", C.c_double), ("pivoting_used", C.c_int32), ("reserved", C.c_int32)]
 
 
 P = C.c_void_p

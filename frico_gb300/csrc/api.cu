@@ -71,6 +71,8 @@ static int check_options(frico_gpu_ctx* ctx, const frico_gpu_options* o) {
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown h_phase_mode");
     if (o->gemm_engine < FRICO_GEMM_AUTO || o->gemm_engine > FRICO_GEMM_TC)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown gemm_engine");
+    if (o->pivoting < FRICO_PIVOT_AUTO || o->pivoting > FRICO_PIVOT_NONE)
+        return set_err(ctx, FRICO_GPU_EINVAL, "unknown pivoting");
     return FRICO_GPU_OK;
 }
 
@@ -139,7 +141,8 @@ extern "C" int frico_gpu_set_options(frico_gpu_ctx* ctx, const frico_gpu_options
     int rc = check_options(ctx, opt);
     if (rc) return rc;
     bool refill = opt->degree != ctx->opt.degree || opt->approx != ctx->opt.approx ||
-                  opt->force_symmetry != ctx->opt.force_symmetry || opt->precision != ctx->opt.precision;
+                  opt->force_symmetry != ctx->opt.force_symmetry || opt->precision != ctx->opt.precision ||
+                  opt->pivoting != ctx->opt.pivoting || opt->gemm_engine != ctx->opt.gemm_engine;
     ctx->opt = *opt;
     if (ctx->opt.Z0 == 0.0) ctx->opt.Z0 = 50.0;
     if (refill) {
@@ -319,11 +322,29 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
     if (ctx->nrhs <= 0) return set_err(ctx, FRICO_GPU_ESTATE, "solve: no right-hand sides");
     if (I_out && ldi < ctx->n) return set_err(ctx, FRICO_GPU_EINVAL, "solve: ldi < n");
     const bool mixed = ctx->opt.precision == FRICO_PREC_MIXED;
+    const int piv = ctx->opt.pivoting;
     int rc;
+    // mixed precision, complex64 factors: without interchanges first (FRICO_PIVOT_AUTO / NONE),
+    // partial pivoting when a pivot vanishes or (below) the refinement does not converge
+    auto factor_mixed = [&](bool partial) -> int {
+        StageTimer tm(ctx, &ctx->stats.factor_ms);
+        int r = partial ? lu_factor_fp32(ctx) : lu_factor_nopiv_fp32(ctx);
+        ctx->stats.pivoting_used = partial ? FRICO_PIVOT_PARTIAL : FRICO_PIVOT_NONE;
+        return r;
+    };
     if (!ctx->factored || ctx->factor_prec != ctx->opt.precision) {
         if (!ctx->z_valid) return set_err(ctx, FRICO_GPU_ESTATE, "solve: no impedance matrix (call fill)");
-        StageTimer tm(ctx, &ctx->stats.factor_ms);
-        rc = mixed ? lu_factor_fp32(ctx) : lu_factor_fp64(ctx);
+        if (mixed) {
+            rc = factor_mixed(piv == FRICO_PIVOT_PARTIAL);
+            if (!rc && ctx->info != 0 && piv == FRICO_PIVOT_AUTO) {
+                if ((rc = z64_to_z32(ctx))) return rc;
+                rc = factor_mixed(true);
+            }
+        } else {
+            StageTimer tm(ctx, &ctx->stats.factor_ms);
+            rc = lu_factor_fp64(ctx);
+            ctx->stats.pivoting_used = FRICO_PIVOT_PARTIAL;
+        }
         if (rc) return rc;
         ctx->factored = true;
         ctx->factor_prec = ctx->opt.precision;
@@ -340,8 +361,21 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
     ctx->stats.refine_residual = 0.0;
     const int64_t n = ctx->n;
     if (mixed) {
-        StageTimer tm(ctx, &ctx->stats.refine_ms);
-        rc = refine_solve(ctx);
+        {
+            StageTimer tm(ctx, &ctx->stats.refine_ms);
+            rc = refine_solve(ctx);
+        }
+        if (rc == FRICO_GPU_ENOCONV && piv == FRICO_PIVOT_AUTO && ctx->stats.pivoting_used == FRICO_PIVOT_NONE) {
+            int rc2 = z64_to_z32(ctx);
+            if (!rc2) rc2 = factor_mixed(true);
+            if (rc2) return rc2;
+            if (ctx->info != 0) {
+                if (info) *info = ctx->info;
+                return set_err(ctx, FRICO_GPU_ESINGULAR, "singular matrix (complex64 factorisation)");
+            }
+            StageTimer tm(ctx, &ctx->stats.refine_ms);
+            rc = refine_solve(ctx);
+        }
         ctx->stats.solve_ms = 0.0;
     } else {
         ctx->stats.refine_ms = 0.0;

@@ -179,6 +179,11 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
                    const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev);  // gemm_tc.cu
 int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                        const float2* U, int64_t ldu, int m, int n, int k);  // lu.cu
+int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce);  // lu.cu
+cudaEvent_t* prof_event_pair(frico_gpu_ctx* ctx);            // lu.cu
+void prof_event_collect(frico_gpu_ctx* ctx);                  // lu.cu
+int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx);                 // lu_nopiv.cu
+int z64_to_z32(frico_gpu_ctx* ctx);                           // fill.cu
 int rhs_delta_gap(frico_gpu_ctx* ctx, double freq, int col, int n_itf, const int32_t* tags,
                   double2 V0, const double* signs);           // fields.cu
 int rhs_plane_wave(frico_gpu_ctx* ctx, double freq, int col, double theta, double phi,

@@ -568,6 +568,18 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     return FRICO_GPU_OK;
 }
 
+// Z32 <- complex64(Z64): rebuilds the mixed-precision copy (e.g. before a
+// second factorisation with a different pivoting strategy).
+int z64_to_z32(frico_gpu_ctx* ctx) {
+    const int64_t n = ctx->n, cnt = n * n;
+    int rc;
+    if ((rc = ensure(ctx, ctx->z32, sizeof(float2) * size_t(cnt)))) return rc;
+    k_z64_to_z32<<<unsigned((cnt + 255) / 256), 256, 0, ctx->stream>>>(cnt, (const double2*)ctx->z64.p,
+                                                                       (float2*)ctx->z32.p);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_z64_to_z32");
+}
+
 int symmetrize(frico_gpu_ctx* ctx) {
     int64_t n = ctx->n;
     unsigned nb = unsigned((n + 31) / 32);

@@ -246,16 +246,24 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int gr = mt * BM + row;
             const uint32_t taddr = tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * BN);
+            // 64 C values of this thread's row are requested before their first
+            // use: 4 warps x 64 coalesced 128-byte requests in flight per SM.
+            const int ncol = min(BN, g.N - nt_ * BN);
+            const bool rowok = gr < g.M;
 #pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                float v[32];
-                tmem_ld32(taddr + uint32_t(c0), v);
-                if (gr < g.M) {
-                    float* cp = g.C + int64_t(nt_ * BN + c0) * g.ldc + gr;
-                    const int ncol = min(32, g.N - (nt_ * BN + c0));
+            for (int h = 0; h < BN; h += 64) {
+                const float* cp = g.C + int64_t(nt_ * BN + h) * g.ldc + gr;
+                float cv[64];
+#pragma unroll
+                for (int j = 0; j < 64; j++) cv[j] = (rowok && h + j < ncol) ? cp[int64_t(j) * g.ldc] : 0.f;
+#pragma unroll
+                for (int c0 = 0; c0 < 64; c0 += 32) {
+                    float v[32];
+                    tmem_ld32(taddr + uint32_t(h + c0), v);
+                    float* wp = g.C + int64_t(nt_ * BN + h + c0) * g.ldc + gr;
 #pragma unroll
                     for (int j = 0; j < 32; j++)
-                        if (j < ncol) cp[int64_t(j) * g.ldc] -= v[j];
+                        if (rowok && h + c0 + j < ncol) wp[int64_t(j) * g.ldc] = cv[c0 + j] - v[j];
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -565,7 +565,7 @@ __global__ void k_add_c64_to_c128(int64_t count, const float2* d, double2* x, in
 // ---------------------------------------------------------------- host side
 // With opt.profile_kernels, every trailing-update GEMM is bracketed by a pair
 // of CUDA events on the context stream; prof_collect() sums their times.
-static cudaEvent_t* prof_pair(frico_gpu_ctx* ctx) {
+cudaEvent_t* prof_event_pair(frico_gpu_ctx* ctx) {
     if (!ctx->opt.profile_kernels) return nullptr;
     if (ctx->prof_used + 2 > ctx->prof_events.size()) {
         for (int k = 0; k < 64; k++) {
@@ -579,7 +579,7 @@ static cudaEvent_t* prof_pair(frico_gpu_ctx* ctx) {
     return p;
 }
 
-static void prof_collect(frico_gpu_ctx* ctx) {
+void prof_event_collect(frico_gpu_ctx* ctx) {
     if (!ctx->prof_used) return;
     cudaEventSynchronize(ctx->prof_events[ctx->prof_used - 1]);
     for (size_t k = 0; k + 1 < ctx->prof_used; k += 2) {
@@ -738,7 +738,7 @@ template <typename R> struct LuDriver {
         const C* Am = A + int64_t(k0) * lda + r0;
         const C* Bm = A + int64_t(c0) * lda + k0;
         dim3 gg((m + 63) / 64, (nn + 63) / 64);
-        cudaEvent_t* ev = profile ? prof_pair(ctx) : nullptr;
+        cudaEvent_t* ev = profile ? prof_event_pair(ctx) : nullptr;
         if (ev) ctx->stats.gemm_flops += 8.0 * double(m) * double(nn) * double(kk);
         if (sizeof(R) == 4 && profile && use_tc && m >= 128 && nn >= 128) {
             // outer trailing update on the tensor cores (events bracket the MMA kernel)
@@ -824,7 +824,7 @@ static int lu_factor_impl(frico_gpu_ctx* ctx, cplx<R>* A) {
     k_perm_from_ipiv<<<1, 1024, sizeof(int32_t) * n, st>>>(n, (const int32_t*)ctx->ipiv.p, (int32_t*)ctx->perm.p);
     count_launch(ctx);
     if ((rc = cuda_check(ctx, cudaGetLastError(), "k_perm_from_ipiv"))) return rc;
-    prof_collect(ctx);
+    prof_event_collect(ctx);
     DeviceStatus hs;
     if ((rc = cuda_check(ctx, cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, st), "status")))
         return rc;
@@ -844,6 +844,23 @@ static int lu_factor_impl(frico_gpu_ctx* ctx, cplx<R>* A) {
 
 int lu_factor_fp64(frico_gpu_ctx* ctx) { return lu_factor_impl<double>(ctx, (double2*)ctx->z64.p); }
 int lu_factor_fp32(frico_gpu_ctx* ctx) { return lu_factor_impl<float>(ctx, (float2*)ctx->z32.p); }
+
+// A[k0:k0+jb, cb:ce] <- L11^{-1} A[k0:k0+jb, cb:ce] (unit lower L11 at (k0, k0)), jb <= 128.
+int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce) {
+    if (ce <= cb) return FRICO_GPU_OK;
+    const size_t smem = sizeof(float2) * (size_t(jb) * jb + 32 * jb);
+    static size_t set_for = 0;
+    if (smem > set_for) {
+        int rc = cuda_check(ctx, cudaFuncSetAttribute(k_trsm_lower_unit<float2>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)),
+                            "trsm smem attribute");
+        if (rc) return rc;
+        set_for = smem;
+    }
+    k_trsm_lower_unit<float2><<<(ce - cb + 31) / 32, 256, smem, ctx->stream>>>(A, lda, k0, jb, cb, ce);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_trsm_lower_unit");
+}
 
 int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl, const float2* U,
                        int64_t ldu, int m, int n, int k) {
@@ -929,6 +946,7 @@ int refine_solve(frico_gpu_ctx* ctx) {
             rel = std::max(rel, std::sqrt(hn[c]) / bn);
         }
         src = Rr;
+        if (!std::isfinite(rel)) { it++; break; }
         if (rel <= tol) { it++; break; }
         if (it >= 2 && rel > 0.5 * prev) { it++; break; }  // stagnation
         prev = rel;

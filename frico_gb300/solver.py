@@ -107,7 +107,7 @@ class Simulation:
                  force_symmetry: bool = False, precision: str = "fp64", Z0: float = 50.0,
                  h_phase: str = "compat", edge_length: str = "xy", device: int = 0,
                  max_refine_iters: int = 30, refine_tol: float = 1e-12, profile_kernels: bool = False,
-                 gemm_engine: str = "auto"):
+                 gemm_engine: str = "auto", pivoting: str = "auto"):
         self.lib = _abi.load()
         self.mesh = mesh
         self.fs = make_function_space(mesh, edge_length)
@@ -115,7 +115,9 @@ class Simulation:
                                 _abi.PREC_MIXED if precision == "mixed" else _abi.PREC_FP64,
                                 _abi.HPHASE_PHYSICAL if h_phase == "physical" else _abi.HPHASE_COMPAT,
                                 max_refine_iters, refine_tol, Z0, int(profile_kernels),
-                                {"auto": _abi.GEMM_AUTO, "simt": _abi.GEMM_SIMT, "tc": _abi.GEMM_TC}[gemm_engine])
+                                {"auto": _abi.GEMM_AUTO, "simt": _abi.GEMM_SIMT, "tc": _abi.GEMM_TC}[gemm_engine],
+                                {"auto": _abi.PIVOT_AUTO, "partial": _abi.PIVOT_PARTIAL,
+                                 "none": _abi.PIVOT_NONE}[pivoting], 0)
         self.ctx = C.c_void_p()
         rc = self.lib.frico_gpu_ctx_create(C.byref(self.ctx), device, C.byref(self.opt))
         _check(self.lib, rc, what="frico_gpu_ctx_create (is a CUDA device visible?)")

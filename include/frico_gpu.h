@@ -88,7 +88,13 @@ typedef struct frico_gpu_options {
     double  Z0;              /* reference impedance for gamma/SWR (-Z)       */
     int32_t profile_kernels; /* 1: CUDA-event timing of every LU update GEMM */
     int32_t gemm_engine;     /* complex64 trailing update: FRICO_GEMM_AUTO or FRICO_GEMM_SIMT */
+    int32_t pivoting;        /* FRICO_PIVOT_* (mixed precision only; FP64 always pivots) */
+    int32_t reserved;
 } frico_gpu_options;
+
+#define FRICO_PIVOT_AUTO    0  /* mixed: no interchanges, partial pivoting if that fails */
+#define FRICO_PIVOT_PARTIAL 1  /* LAPACK zgetrf partial pivoting                        */
+#define FRICO_PIVOT_NONE    2  /* no interchanges (refinement failure is an error)      */
 
 #define FRICO_GEMM_AUTO 0   /* tcgen05 3xTF32 on sm_103, SIMT otherwise */
 #define FRICO_GEMM_SIMT 1   /* CUDA-core FP32 complex GEMM               */
@@ -113,6 +119,8 @@ typedef struct frico_gpu_stats {
     int64_t gemm_launches;       /* LU trailing-update launches timed (profile_kernels) */
     double  gemm_ms;             /* their summed CUDA-event time            */
     double  gemm_flops;          /* their algorithmic real flops (8 m n k)  */
+    int32_t pivoting_used;       /* FRICO_PIVOT_PARTIAL / _NONE of the last factorisation */
+    int32_t reserved;
 } frico_gpu_stats;
 
 typedef struct frico_gpu_ctx frico_gpu_ctx;

@@ -14,7 +14,7 @@ def run(lib, ctx, A, B, Cm, engine):
     n = B.shape[1]
     a = np.asfortranarray(A, np.complex64)
     b = np.asfortranarray(B, np.complex64)
-    c = np.asfortranarray(Cm, np.complex64).copy()
+    c = np.array(Cm, dtype=np.complex64, order="F", copy=True)
     p = lambda x: x.ctypes.data_as(C.c_void_p)  # noqa: E731
     rc = lib.frico_gpu_debug_cgemm(ctx, m, n, k, p(a), p(b), p(c), engine)
     assert rc == 0, lib.frico_gpu_last_error(ctx).decode()

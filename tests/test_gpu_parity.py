@@ -150,6 +150,40 @@ def test_mixed_precision_sphere(gpu_lib):
     assert rel_norm(E, Er) < MIXED_TOL
 
 
+@pytest.mark.parametrize("pivoting,engine", [("auto", "auto"), ("none", "simt"), ("partial", "auto"),
+                                             ("partial", "simt")])
+def test_mixed_pivoting_modes(gpu_lib, pivoting, engine):
+    """Every complex64 factorisation strategy refines to the FP64 solution."""
+    m = meshes.icosphere(3)
+    f = 450e6
+    o = oracle_for(m)
+    Ir = o.solve(o.compute_matrix(f), o.rhs_plane_wave(f, 0.3, 0.1, 1.0, 0.5))
+    sim = Simulation(m, precision="mixed", pivoting=pivoting, gemm_engine=engine)
+    sim.compute_matrix(f)
+    sim.set_nrhs(1)
+    sim.update_rhs(f, PlaneWave(0.3, 0.1, 1.0, 0.5))
+    I = sim.solve()[:, 0]
+    st = sim.stats()
+    assert st["pivoting_used"] == (1 if pivoting == "partial" else 2)
+    assert rel_norm(I, Ir) < MIXED_TOL
+
+
+def test_mixed_singular_falls_back_then_reports(gpu_lib):
+    """A zero pivot in the unpivoted complex64 LU triggers the partial-pivoting
+    fallback; an exactly singular Z then comes back as ESINGULAR with info."""
+    m = meshes.strip_dipole()
+    m.vertices = m.vertices[:, [0, 2, 1]].copy()   # vertical transverse edges: zero-length RWG
+    sim = Simulation(m, precision="mixed")
+    sim.compute_matrix(300e6)
+    sim.set_nrhs(1)
+    sim.update_rhs(300e6, DeltaGap((meshes.FEED_TAG,)))
+    from frico_gb300 import FricoError
+    with pytest.raises(FricoError) as e:
+        sim.solve()
+    assert e.value.code == -2
+    assert sim.stats()["pivoting_used"] == 1
+
+
 def test_mixed_strip_zin(gpu_lib, strip):
     f = 300e6
     o = oracle_for(strip)
