@@ -52,7 +52,8 @@ class Stats(C.Structure):
                 ("fields_ms", C.c_double), ("refine_iters", C.c_int32), ("refine_residual", C.c_double),
                 ("n", C.c_int64), ("ntri", C.c_int64), ("nrhs", C.c_int64), ("green_evals", C.c_int64),
                 ("kernel_launches", C.c_int64), ("gemm_launches", C.c_int64), ("gemm_ms", C.c_double),
-                ("gemm_flops", C.c_double), ("pivoting_used", C.c_int32), ("reserved", C.c_int32)]
+                ("gemm_flops", C.c_double), ("gemm_bytes", C.c_double), ("pivoting_used", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 P = C.c_void_p

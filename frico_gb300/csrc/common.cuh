@@ -176,7 +176,8 @@ int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw);   // 
 int trsv_check(frico_gpu_ctx* ctx);                           // trsv.cu
 bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
-                   const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev);  // gemm_tc.cu
+                   const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev,
+                   int accumulate = 1);                       // gemm_tc.cu
 int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                        const float2* U, int64_t ldu, int m, int n, int k);  // lu.cu
 int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce);  // lu.cu

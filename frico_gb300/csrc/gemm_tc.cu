@@ -140,6 +140,7 @@ struct GemmArgs {
     float* C;          // real view of the complex C: M x N column-major, ld = ldc floats
     int64_t ldc;
     int M, N, KP;      // KP = padded K in floats (multiple of 32)
+    int accumulate;    // 1: C -= A B; 0: C = A B
     DeviceStatus* st;
 };
 
@@ -255,7 +256,8 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
                 const float* cp = g.C + int64_t(nt_ * BN + h) * g.ldc + gr;
                 float cv[64];
 #pragma unroll
-                for (int j = 0; j < 64; j++) cv[j] = (rowok && h + j < ncol) ? cp[int64_t(j) * g.ldc] : 0.f;
+                for (int j = 0; j < 64; j++)
+                    cv[j] = (g.accumulate && rowok && h + j < ncol) ? cp[int64_t(j) * g.ldc] : 0.f;
 #pragma unroll
                 for (int c0 = 0; c0 < 64; c0 += 32) {
                     float v[32];
@@ -263,7 +265,8 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
                     float* wp = g.C + int64_t(nt_ * BN + h + c0) * g.ldc + gr;
 #pragma unroll
                     for (int j = 0; j < 32; j++)
-                        if (rowok && h + c0 + j < ncol) wp[int64_t(j) * g.ldc] = cv[c0 + j] - v[j];
+                        if (rowok && h + c0 + j < ncol)
+                            wp[int64_t(j) * g.ldc] = g.accumulate ? cv[c0 + j] - v[j] : v[j];
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -367,9 +370,11 @@ bool gemm_tc_available(frico_gpu_ctx* ctx) {
     return major == 10 && minor == 3 && encode_fn() != nullptr;
 }
 
-// C[m x n] -= L[m x k] * U[k x n], complex64 column-major, leading dims ldc, ldl, ldu.
+// C[m x n] -= L[m x k] * U[k x n] (accumulate = 1) or C = L U (accumulate = 0),
+// complex64 column-major, leading dims ldc, ldl, ldu. C may alias L or U: both
+// operands are copied (split) before the MMA kernel writes C.
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl, const float2* U,
-                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev) {
+                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev, int accumulate) {
     if (m <= 0 || n <= 0 || k <= 0) return FRICO_GPU_OK;
     const int KP = ((2 * k + tc::BK - 1) / tc::BK) * tc::BK;
     const int M = 2 * m;
@@ -404,6 +409,7 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     ga.M = M;
     ga.N = n;
     ga.KP = KP;
+    ga.accumulate = accumulate;
     ga.st = (DeviceStatus*)ctx->status.p;
     if (ev) cudaEventRecord(ev[0], st);
     tc::k_gemm_tf32x3<<<std::min(ntiles, sms), 192, tc::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);

@@ -188,9 +188,11 @@ __global__ void __launch_bounds__(256) k_panel(cplx<R>* A, int64_t lda, int n, i
         __syncthreads();
         const int nrr = nr - rs, ncols = jb - c - 1;
         if (nrr > 0)
-            for (int idx = tid; idx < nrr * ncols; idx += blockDim.x) {
-                int r = rs + idx % nrr, cc = c + 1 + idx / nrr;
-                sm[cc * rows_per + r] = cfms(sm[cc * rows_per + r], sm[c * rows_per + r], prow[cc]);
+            // thread = (row lane of 64, column group of 4): no integer division
+            for (int cc = c + 1 + (tid >> 6); cc < jb; cc += 4) {
+                const C u = prow[cc];
+                for (int r = rs + (tid & 63); r < nr; r += 64)
+                    sm[cc * rows_per + r] = cfms(sm[cc * rows_per + r], sm[c * rows_per + r], u);
             }
         __syncthreads();
         if (c + 1 < jb) {
@@ -306,9 +308,11 @@ __global__ void __launch_bounds__(256) k_panel_cluster(cplx<R>* A, int64_t lda, 
         __syncthreads();
         const int nrr = nr - rs, ncols = jb - c - 1;
         if (nrr > 0)
-            for (int idx = tid; idx < nrr * ncols; idx += blockDim.x) {
-                int r = rs + idx % nrr, cc = c + 1 + idx / nrr;
-                sm[cc * rows_per + r] = cfms(sm[cc * rows_per + r], sm[c * rows_per + r], prow[cc]);
+            // thread = (row lane of 64, column group of 4): no integer division
+            for (int cc = c + 1 + (tid >> 6); cc < jb; cc += 4) {
+                const C u = prow[cc];
+                for (int r = rs + (tid & 63); r < nr; r += 64)
+                    sm[cc * rows_per + r] = cfms(sm[cc * rows_per + r], sm[c * rows_per + r], u);
             }
         __syncthreads();
         if (c + 1 < jb) publish(c + 1, par ^ 1);
@@ -739,7 +743,10 @@ template <typename R> struct LuDriver {
         const C* Bm = A + int64_t(c0) * lda + k0;
         dim3 gg((m + 63) / 64, (nn + 63) / 64);
         cudaEvent_t* ev = profile ? prof_event_pair(ctx) : nullptr;
-        if (ev) ctx->stats.gemm_flops += 8.0 * double(m) * double(nn) * double(kk);
+        if (ev) {
+            ctx->stats.gemm_flops += 8.0 * double(m) * double(nn) * double(kk);
+            ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(m) * double(nn) + double(m + nn) * kk);
+        }
         if (sizeof(R) == 4 && profile && use_tc && m >= 128 && nn >= 128) {
             // outer trailing update on the tensor cores (events bracket the MMA kernel)
             int rc = gemm_update_tc(ctx, (float2*)Cm, lda, (const float2*)Am, lda, (const float2*)Bm, lda, m, nn,

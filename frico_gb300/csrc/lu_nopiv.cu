@@ -29,63 +29,88 @@ static const int kNP = 128;   // block width of the no-pivot LU
 
 template <typename C> __device__ __forceinline__ bool cfinite(C a) { return isfinite(a.x) && isfinite(a.y); }
 
-// LU (no interchanges) of the jb x jb diagonal block at (k0, k0), written back
-// in place; U11^{-1} (upper) to Uinv (jb x jb, column-major, ld jb).
+// In-place inverse of the upper triangle of the jb x jb column-major block a
+// (entries below the diagonal are neither read nor written). With unit = 1 the
+// diagonal is taken as 1. Column j of the inverse needs only columns < j:
+//   X[j][j] = 1/U[j][j],  X[i][j] = -(sum_{k=i}^{j-1} X[i][k] U[k][j]) X[j][j]
+// 512 threads: thread (i, g) sums the k = g mod 4 terms of row i.
 template <typename C>
-__global__ void __launch_bounds__(512) k_diag_lu(C* A, int64_t lda, int k0, int jb, C* Uinv, DeviceStatus* st) {
+__device__ void upper_inverse_inplace(C* a, int jb, bool unit, C (*red)[kNP]) {
+    using R = decltype(a[0].x);
+    const int i = threadIdx.x & (kNP - 1), g = threadIdx.x >> 7;
+    for (int j = 0; j < jb; j++) {
+        const C xjj = unit ? cmake(R(1), R(0)) : cdiv(cmake(R(1), R(0)), a[j * jb + j]);
+        C s = cmake(R(0), R(0));
+        if (i < j)
+            for (int k = i + g; k < j; k += 4) {
+                const C xik = (k == i) ? (unit ? cmake(R(1), R(0)) : a[i * jb + i]) : a[k * jb + i];
+                s = cadd(s, cmul(xik, a[j * jb + k]));
+            }
+        red[g][i] = s;
+        __syncthreads();
+        if (g == 0) {
+            if (i < j) {
+                C t = cadd(cadd(red[0][i], red[1][i]), cadd(red[2][i], red[3][i]));
+                a[j * jb + i] = cmul(cmake(-t.x, -t.y), xjj);
+            } else if (i == j && !unit) {
+                a[j * jb + j] = xjj;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// LU (no interchanges) of the jb x jb diagonal block at (k0, k0), written back
+// in place; then U11^{-1} (upper) to Uinv and L11^{-1} (unit lower) to Linv,
+// both jb x jb column-major with leading dimension jb. 512 threads: thread
+// (row r, column group g) updates columns c+1+g, c+5+g, ... of row r.
+template <typename C>
+__global__ void __launch_bounds__(512) k_diag_lu(C* A, int64_t lda, int k0, int jb, C* Uinv, C* Linv,
+                                                DeviceStatus* st) {
     using R = decltype(A[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
     C* a = (C*)smraw;   // a[c * jb + r]
-    __shared__ C inv_s;
+    __shared__ C red[4][kNP];
     for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
         int r = idx % jb, c = idx / jb;
         a[idx] = A[int64_t(k0 + c) * lda + k0 + r];
     }
     __syncthreads();
+    const int r = threadIdx.x & (kNP - 1), g = threadIdx.x >> 7;
     for (int c = 0; c < jb; c++) {
-        if (threadIdx.x == 0) {
-            C p = a[c * jb + c];
-            if ((p.x == R(0) && p.y == R(0)) || !cfinite(p)) {
-                atomicCAS(&st->info, 0, k0 + c + 1);
-                inv_s = cmake(R(0), R(0));
-            } else {
-                inv_s = cdiv(cmake(R(1), R(0)), p);
-            }
-        }
+        const C p = a[c * jb + c];
+        const bool bad = (p.x == R(0) && p.y == R(0)) || !cfinite(p);
+        const C inv = bad ? cmake(R(0), R(0)) : cdiv(cmake(R(1), R(0)), p);
+        if (bad && threadIdx.x == 0) atomicCAS(&st->info, 0, k0 + c + 1);
+        if (g == 0 && r > c && r < jb) a[c * jb + r] = cmul(a[c * jb + r], inv);
         __syncthreads();
-        const C inv = inv_s;
-        for (int r = c + 1 + threadIdx.x; r < jb; r += blockDim.x) a[c * jb + r] = cmul(a[c * jb + r], inv);
-        __syncthreads();
-        const int nr = jb - c - 1;
-        for (int idx = threadIdx.x; idx < nr * nr; idx += blockDim.x) {
-            int r = c + 1 + idx % nr, cc = c + 1 + idx / nr;
-            a[cc * jb + r] = cfms(a[cc * jb + r], a[c * jb + r], a[cc * jb + c]);
+        if (r > c && r < jb) {
+            const C l = a[c * jb + r];
+            for (int cc = c + 1 + g; cc < jb; cc += 4) a[cc * jb + r] = cfms(a[cc * jb + r], l, a[cc * jb + c]);
         }
         __syncthreads();
     }
     for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int r = idx % jb, c = idx / jb;
-        A[int64_t(k0 + c) * lda + k0 + r] = a[idx];
+        int rr = idx % jb, c = idx / jb;
+        A[int64_t(k0 + c) * lda + k0 + rr] = a[idx];
     }
-    // U^{-1} in place, column by column: X[j][j] = 1/U[j][j],
-    // X[i][j] = -(sum_{k=i}^{j-1} X[i][k] U[k][j]) X[j][j] for i < j.
-    // Column j of U is read before it is overwritten (all threads finish the
-    // sums before the __syncthreads that precedes the writes).
-    for (int j = 0; j < jb; j++) {
-        C xjj = cdiv(cmake(R(1), R(0)), a[j * jb + j]);
-        C s = cmake(R(0), R(0));
-        const int i = threadIdx.x;
-        if (i < j)
-            for (int k = i; k < j; k++) s = cadd(s, cmul(a[k * jb + i], a[j * jb + k]));
-        __syncthreads();
-        if (i < j) a[j * jb + i] = cmul(cmake(-s.x, -s.y), xjj);
-        if (i == j) a[j * jb + j] = xjj;
-        // entries below the diagonal (the L part) are not part of U^{-1}
-        __syncthreads();
-    }
+    upper_inverse_inplace(a, jb, false, red);
     for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int r = idx % jb, c = idx / jb;
-        Uinv[idx] = r <= c ? a[idx] : cmake(R(0), R(0));
+        int rr = idx % jb, c = idx / jb;
+        Uinv[idx] = rr <= c ? a[idx] : cmake(R(0), R(0));
+    }
+    __syncthreads();
+    // L^{-1} = ((L^T)^{-1})^T: reload the factored block transposed, so that
+    // L^T sits in the upper triangle, and invert it with unit diagonal.
+    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
+        int rr = idx % jb, c = idx / jb;               // global (row rr, col c)
+        a[rr * jb + c] = A[int64_t(k0 + c) * lda + k0 + rr];
+    }
+    __syncthreads();
+    upper_inverse_inplace(a, jb, true, red);
+    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
+        int rr = idx % jb, c = idx / jb;               // Linv (row rr, col c) = Tinv (row c, col rr)
+        Linv[idx] = rr > c ? a[rr * jb + c] : (rr == c ? cmake(R(1), R(0)) : cmake(R(0), R(0)));
     }
 }
 
@@ -148,10 +173,11 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     if ((rc = ensure(ctx, ctx->ipiv, sizeof(int32_t) * n))) return rc;
     if ((rc = ensure(ctx, ctx->perm, sizeof(int32_t) * n))) return rc;
     if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
-    if ((rc = ensure(ctx, ctx->panel_ws, sizeof(C) * kNP * kNP + 256))) return rc;
+    if ((rc = ensure(ctx, ctx->panel_ws, sizeof(C) * 2 * kNP * kNP + 256))) return rc;
     if ((rc = cuda_check(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(DeviceStatus), st), "status"))) return rc;
     DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
     C* Uinv = (C*)ctx->panel_ws.p;
+    C* Linv = Uinv + kNP * kNP;
     const size_t diag_smem = sizeof(C) * kNP * kNP;
     const size_t right_smem = sizeof(C) * (kNP * kNP + 64 * kNP);
     static bool attrs = false;
@@ -171,19 +197,30 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     count_launch(ctx);
     for (int k0 = 0; k0 < n; k0 += kNP) {
         const int jb = std::min(kNP, n - k0);
-        k_diag_lu<C><<<1, 512, sizeof(C) * jb * jb, st>>>(A, lda, k0, jb, Uinv, dst);
+        k_diag_lu<C><<<1, 512, sizeof(C) * jb * jb, st>>>(A, lda, k0, jb, Uinv, Linv, dst);
         count_launch(ctx);
         const int rest = n - k0 - jb;
         if (rest > 0) {
-            k_trsm_right<C><<<(rest + 63) / 64, 256, sizeof(C) * (jb * jb + 64 * jb), st>>>(A, lda, k0 + jb, n, k0,
-                                                                                            jb, Uinv);
-            count_launch(ctx);
-            if ((rc = trsm_lower_unit_f32(ctx, A, lda, k0, jb, k0 + jb, n))) return rc;
+            C* A21 = A + int64_t(k0) * lda + k0 + jb;
+            C* A12 = A + int64_t(k0 + jb) * lda + k0;
+            if (tc) {
+                // L21 = A21 U11^{-1},  U12 = L11^{-1} A12 on the tensor cores (overwrite mode)
+                if ((rc = gemm_update_tc(ctx, A21, lda, A21, lda, Uinv, jb, rest, jb, jb, nullptr, 0))) return rc;
+                if ((rc = gemm_update_tc(ctx, A12, lda, Linv, jb, A12, lda, jb, rest, jb, nullptr, 0))) return rc;
+            } else {
+                k_trsm_right<C><<<(rest + 63) / 64, 256, sizeof(C) * (jb * jb + 64 * jb), st>>>(A, lda, k0 + jb, n,
+                                                                                                k0, jb, Uinv);
+                count_launch(ctx);
+                if ((rc = trsm_lower_unit_f32(ctx, A, lda, k0, jb, k0 + jb, n))) return rc;
+            }
             C* Cm = A + int64_t(k0 + jb) * lda + k0 + jb;
             const C* Lm = A + int64_t(k0) * lda + k0 + jb;
             const C* Um = A + int64_t(k0 + jb) * lda + k0;
             cudaEvent_t* ev = prof_event_pair(ctx);
-            if (ev) ctx->stats.gemm_flops += 8.0 * double(rest) * double(rest) * double(jb);
+            if (ev) {
+                ctx->stats.gemm_flops += 8.0 * double(rest) * double(rest) * double(jb);
+                ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(rest) + 2.0 * double(rest) * jb);
+            }
             if (tc) {
                 if ((rc = gemm_update_tc(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb, ev))) return rc;
             } else {

@@ -119,6 +119,7 @@ typedef struct frico_gpu_stats {
     int64_t gemm_launches;       /* LU trailing-update launches timed (profile_kernels) */
     double  gemm_ms;             /* their summed CUDA-event time            */
     double  gemm_flops;          /* their algorithmic real flops (8 m n k)  */
+    double  gemm_bytes;          /* their algorithmic bytes: C read+write + L, U reads */
     int32_t pivoting_used;       /* FRICO_PIVOT_PARTIAL / _NONE of the last factorisation */
     int32_t reserved;
 } frico_gpu_stats;
