@@ -10,8 +10,8 @@
 // pivot is zero / not finite (info != 0) or the refinement does not converge.
 //
 // Per block column k0 (width nb = 128):
-//   k_diag_lu      one CTA: LU of the nb x nb diagonal block in shared memory,
-//                  then U11^{-1} (triangular inverse) into a workspace
+//   k_diag_lu      one CTA: LU of the nb x nb diagonal block in registers,
+//                  then U11^{-1} and L11^{-1} (triangular inverses) into a workspace
 //   k_trsm_right   L21 = A21 U11^{-1}, 64 rows per CTA
 //   k_trsm_lower_unit (lu.cu)   U12 = L11^{-1} A12
 //   trailing update A22 -= L21 U12 (tensor cores when available)
@@ -29,88 +29,217 @@ static const int kNP = 128;   // block width of the no-pivot LU
 
 template <typename C> __device__ __forceinline__ bool cfinite(C a) { return isfinite(a.x) && isfinite(a.y); }
 
-// In-place inverse of the upper triangle of the jb x jb column-major block a
-// (entries below the diagonal are neither read nor written). With unit = 1 the
-// diagonal is taken as 1. Column j of the inverse needs only columns < j:
-//   X[j][j] = 1/U[j][j],  X[i][j] = -(sum_{k=i}^{j-1} X[i][k] U[k][j]) X[j][j]
-// 512 threads: thread (i, g) sums the k = g mod 4 terms of row i.
-template <typename C>
-__device__ void upper_inverse_inplace(C* a, int jb, bool unit, C (*red)[kNP]) {
-    using R = decltype(a[0].x);
-    const int i = threadIdx.x & (kNP - 1), g = threadIdx.x >> 7;
-    for (int j = 0; j < jb; j++) {
-        const C xjj = unit ? cmake(R(1), R(0)) : cdiv(cmake(R(1), R(0)), a[j * jb + j]);
-        C s = cmake(R(0), R(0));
-        if (i < j)
-            for (int k = i + g; k < j; k += 4) {
-                const C xik = (k == i) ? (unit ? cmake(R(1), R(0)) : a[i * jb + i]) : a[k * jb + i];
-                s = cadd(s, cmul(xik, a[j * jb + k]));
-            }
-        red[g][i] = s;
-        __syncthreads();
-        if (g == 0) {
-            if (i < j) {
-                C t = cadd(cadd(red[0][i], red[1][i]), cadd(red[2][i], red[3][i]));
-                a[j * jb + i] = cmul(cmake(-t.x, -t.y), xjj);
-            } else if (i == j && !unit) {
-                a[j * jb + j] = xjj;
-            }
+// Diagonal block kernel: 256 threads as a 16 x 16 grid; thread (tx, ty) keeps
+// rows ty + 16 i and columns tx + 16 j (i, j < 8) of the 128 x 128 block in
+// registers. Every elimination step is a rank-1 update of the registers from
+// one column and one row published in shared memory (double-buffered, so one
+// barrier per step). Step c lies in phase P = c / 16; rows and columns of the
+// register tile below P are finished, so each phase is unrolled for its own P
+// and does only the live part of the tile.
+static const int kDLD = kNP + 1;   // shared leading dimension (conflict-free tile reads)
+
+// LU (no interchanges), steps c = 16 P .. 16 P + 15. rdiag[c] = 1 / pivot.
+template <int P, typename C>
+__device__ __forceinline__ void diag_lu_phase(C (&v)[8][8], C* vb, C* rdiag, int tx, int ty, int k0,
+                                              DeviceStatus* st) {
+    using R = decltype(v[0][0].x);
+#pragma unroll 1
+    for (int cl = 0; cl < 16; cl++) {
+        const int c = 16 * P + cl;
+        C* lb = vb + (c & 1) * 2 * kNP;   // column c (rows below the pivot)
+        C* ub = lb + kNP;                 // row c (pivot and right of it)
+        if (tx == cl) {
+#pragma unroll
+            for (int i = P; i < 8; i++) lb[ty + 16 * i] = v[i][P];
+        }
+        if (ty == cl) {
+#pragma unroll
+            for (int j = P; j < 8; j++) ub[tx + 16 * j] = v[P][j];
         }
         __syncthreads();
+        const C p = ub[c];
+        const bool bad = (p.x == R(0) && p.y == R(0)) || !cfinite(p);
+        const R d = p.x * p.x + p.y * p.y;
+        const C inv = bad ? cmake(R(0), R(0)) : cmake(p.x / d, -p.y / d);
+        if (threadIdx.x == 0) {
+            rdiag[c] = inv;
+            if (bad) atomicCAS(&st->info, 0, k0 + c + 1);
+        }
+        C l[8], u[8];
+#pragma unroll
+        for (int i = P; i < 8; i++) l[i] = (i > P || ty > cl) ? cmul(lb[ty + 16 * i], inv) : cmake(R(0), R(0));
+#pragma unroll
+        for (int j = P; j < 8; j++) u[j] = (j > P || tx > cl) ? ub[tx + 16 * j] : cmake(R(0), R(0));
+#pragma unroll
+        for (int i = P; i < 8; i++)
+#pragma unroll
+            for (int j = P; j < 8; j++) v[i][j] = cfms(v[i][j], l[i], u[j]);
+        if (tx == cl) {
+#pragma unroll
+            for (int i = P; i < 8; i++)
+                if (i > P || ty > cl) v[i][P] = l[i];
+        }
     }
 }
 
+// X = U^{-1} by backward column sweeps, steps i = 16 P + 15 .. 16 P:
+//   X[i,:] /= U[i][i];  X[k,:] -= U[k][i] X[i,:]  (k < i).
+// X[i][j] = 0 for j < i, so only tile columns >= P and rows <= P are live.
+template <int P, typename C>
+__device__ __forceinline__ void diag_uinv_phase(C (&x)[8][8], const C* S, C* vb, const C* rdiag, int tx, int ty,
+                                                int& step) {
+    using R = decltype(x[0][0].x);
+#pragma unroll 1
+    for (int il = 15; il >= 0; il--) {
+        const int i = 16 * P + il;
+        C* b = vb + (step++ & 1) * kNP;
+        if (ty == il) {
+#pragma unroll
+            for (int j = P; j < 8; j++) b[tx + 16 * j] = x[P][j];
+        }
+        __syncthreads();
+        const C inv = rdiag[i];
+        C xr[8], cf[8];
+#pragma unroll
+        for (int j = P; j < 8; j++) xr[j] = cmul(b[tx + 16 * j], inv);
+#pragma unroll
+        for (int k = 0; k <= P; k++) cf[k] = (k < P || ty < il) ? S[i * kDLD + ty + 16 * k] : cmake(R(0), R(0));
+#pragma unroll
+        for (int k = 0; k <= P; k++)
+#pragma unroll
+            for (int j = P; j < 8; j++) x[k][j] = cfms(x[k][j], cf[k], xr[j]);
+        if (ty == il) {
+#pragma unroll
+            for (int j = P; j < 8; j++) x[P][j] = xr[j];
+        }
+    }
+}
+
+// Y = L^{-1} (unit lower) by forward column sweeps, steps i = 16 P .. 16 P + 15:
+//   Y[k,:] -= L[k][i] Y[i,:]  (k > i).  Live: tile rows >= P, columns <= P.
+template <int P, typename C>
+__device__ __forceinline__ void diag_linv_phase(C (&y)[8][8], const C* S, C* vb, int tx, int ty, int& step) {
+    using R = decltype(y[0][0].x);
+#pragma unroll 1
+    for (int il = 0; il < 16; il++) {
+        const int i = 16 * P + il;
+        C* b = vb + (step++ & 1) * kNP;
+        if (ty == il) {
+#pragma unroll
+            for (int j = 0; j <= P; j++) b[tx + 16 * j] = y[P][j];
+        }
+        __syncthreads();
+        C yr[8], cf[8];
+#pragma unroll
+        for (int j = 0; j <= P; j++) yr[j] = b[tx + 16 * j];
+#pragma unroll
+        for (int k = P; k < 8; k++) cf[k] = (k > P || ty > il) ? S[i * kDLD + ty + 16 * k] : cmake(R(0), R(0));
+#pragma unroll
+        for (int k = P; k < 8; k++)
+#pragma unroll
+            for (int j = 0; j <= P; j++) y[k][j] = cfms(y[k][j], cf[k], yr[j]);
+    }
+}
+
+template <typename C> constexpr size_t diag_lu_smem() { return sizeof(C) * (size_t(kNP) * kDLD + 5 * kNP); }
+
 // LU (no interchanges) of the jb x jb diagonal block at (k0, k0), written back
-// in place; then U11^{-1} (upper) to Uinv and L11^{-1} (unit lower) to Linv,
-// both jb x jb column-major with leading dimension jb. 512 threads: thread
-// (row r, column group g) updates columns c+1+g, c+5+g, ... of row r.
+// in place; U11^{-1} to Uinv and L11^{-1} (unit lower) to Linv, both jb x jb
+// column-major with leading dimension jb. A block narrower than 128 is padded
+// with the identity. A zero or non-finite pivot sets st->info (first one).
 template <typename C>
-__global__ void __launch_bounds__(512) k_diag_lu(C* A, int64_t lda, int k0, int jb, C* Uinv, C* Linv,
+__global__ void __launch_bounds__(256) k_diag_lu(C* A, int64_t lda, int k0, int jb, C* Uinv, C* Linv,
                                                 DeviceStatus* st) {
     using R = decltype(A[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
-    C* a = (C*)smraw;   // a[c * jb + r]
-    __shared__ C red[4][kNP];
-    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int r = idx % jb, c = idx / jb;
-        a[idx] = A[int64_t(k0 + c) * lda + k0 + r];
+    C* S = (C*)smraw;              // S[c * kDLD + r]
+    C* vb = S + kNP * kDLD;        // 4 x kNP published rows / columns
+    C* rdiag = vb + 4 * kNP;       // reciprocal pivots
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll 16
+    for (int it = 0; it < kNP * kNP / 256; it++) {
+        const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        S[c * kDLD + r] = (r < jb && c < jb) ? A[int64_t(k0 + c) * lda + k0 + r] : cmake(R(r == c ? 1 : 0), R(0));
     }
     __syncthreads();
-    const int r = threadIdx.x & (kNP - 1), g = threadIdx.x >> 7;
-    for (int c = 0; c < jb; c++) {
-        const C p = a[c * jb + c];
-        const bool bad = (p.x == R(0) && p.y == R(0)) || !cfinite(p);
-        const C inv = bad ? cmake(R(0), R(0)) : cdiv(cmake(R(1), R(0)), p);
-        if (bad && threadIdx.x == 0) atomicCAS(&st->info, 0, k0 + c + 1);
-        if (g == 0 && r > c && r < jb) a[c * jb + r] = cmul(a[c * jb + r], inv);
-        __syncthreads();
-        if (r > c && r < jb) {
-            const C l = a[c * jb + r];
-            for (int cc = c + 1 + g; cc < jb; cc += 4) a[cc * jb + r] = cfms(a[cc * jb + r], l, a[cc * jb + c]);
+    {
+        C v[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[i][j] = S[(tx + 16 * j) * kDLD + ty + 16 * i];
+        diag_lu_phase<0>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<1>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<2>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<3>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<4>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<5>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<6>(v, vb, rdiag, tx, ty, k0, st);
+        diag_lu_phase<7>(v, vb, rdiag, tx, ty, k0, st);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
+    }
+    __syncthreads();
+#pragma unroll 16
+    for (int it = 0; it < kNP * kNP / 256; it++) {
+        const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        if (r < jb && c < jb) A[int64_t(k0 + c) * lda + k0 + r] = S[c * kDLD + r];
+    }
+    int step = 0;
+    {
+        C x[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) x[i][j] = cmake(R(ty + 16 * i == tx + 16 * j ? 1 : 0), R(0));
+        diag_uinv_phase<7>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<6>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<5>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<4>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<3>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<2>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<1>(x, S, vb, rdiag, tx, ty, step);
+        diag_uinv_phase<0>(x, S, vb, rdiag, tx, ty, step);
+        __syncthreads();   // U no longer read: its triangle of S takes U^{-1}
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = x[i][j];
+    }
+    {
+        C y[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) y[i][j] = cmake(R(ty + 16 * i == tx + 16 * j ? 1 : 0), R(0));
+        diag_linv_phase<0>(y, S, vb, tx, ty, step);
+        diag_linv_phase<1>(y, S, vb, tx, ty, step);
+        diag_linv_phase<2>(y, S, vb, tx, ty, step);
+        diag_linv_phase<3>(y, S, vb, tx, ty, step);
+        diag_linv_phase<4>(y, S, vb, tx, ty, step);
+        diag_linv_phase<5>(y, S, vb, tx, ty, step);
+        diag_linv_phase<6>(y, S, vb, tx, ty, step);
+        diag_linv_phase<7>(y, S, vb, tx, ty, step);
+        __syncthreads();   // L no longer read: the strict lower triangle of S takes L^{-1}
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (ty + 16 * i > tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = y[i][j];
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int it = 0; it < kNP * kNP / 256; it++) {
+        const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        if (r < jb && c < jb) {
+            const C s = S[c * kDLD + r];
+            const C z = cmake(R(0), R(0));
+            Uinv[c * jb + r] = r <= c ? s : z;
+            Linv[c * jb + r] = r > c ? s : (r == c ? cmake(R(1), R(0)) : z);
         }
-        __syncthreads();
-    }
-    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int rr = idx % jb, c = idx / jb;
-        A[int64_t(k0 + c) * lda + k0 + rr] = a[idx];
-    }
-    upper_inverse_inplace(a, jb, false, red);
-    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int rr = idx % jb, c = idx / jb;
-        Uinv[idx] = rr <= c ? a[idx] : cmake(R(0), R(0));
-    }
-    __syncthreads();
-    // L^{-1} = ((L^T)^{-1})^T: reload the factored block transposed, so that
-    // L^T sits in the upper triangle, and invert it with unit diagonal.
-    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int rr = idx % jb, c = idx / jb;               // global (row rr, col c)
-        a[rr * jb + c] = A[int64_t(k0 + c) * lda + k0 + rr];
-    }
-    __syncthreads();
-    upper_inverse_inplace(a, jb, true, red);
-    for (int idx = threadIdx.x; idx < jb * jb; idx += blockDim.x) {
-        int rr = idx % jb, c = idx / jb;               // Linv (row rr, col c) = Tinv (row c, col rr)
-        Linv[idx] = rr > c ? a[rr * jb + c] : (rr == c ? cmake(R(1), R(0)) : cmake(R(0), R(0)));
     }
 }
 
@@ -178,7 +307,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
     C* Uinv = (C*)ctx->panel_ws.p;
     C* Linv = Uinv + kNP * kNP;
-    const size_t diag_smem = sizeof(C) * kNP * kNP;
+    const size_t diag_smem = diag_lu_smem<C>();
     const size_t right_smem = sizeof(C) * (kNP * kNP + 64 * kNP);
     static bool attrs = false;
     if (!attrs) {
@@ -197,7 +326,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     count_launch(ctx);
     for (int k0 = 0; k0 < n; k0 += kNP) {
         const int jb = std::min(kNP, n - k0);
-        k_diag_lu<C><<<1, 512, sizeof(C) * jb * jb, st>>>(A, lda, k0, jb, Uinv, Linv, dst);
+        k_diag_lu<C><<<1, 256, diag_smem, st>>>(A, lda, k0, jb, Uinv, Linv, dst);
         count_launch(ctx);
         const int rest = n - k0 - jb;
         if (rest > 0) {

@@ -74,29 +74,43 @@ __global__ void __launch_bounds__(128) k_invert_diag(const C* __restrict__ LU, i
 }
 
 // W <- T^{-1} W for T = unit-lower L (LOWER) or upper U, nrhs <= kRc.
+// Critical path per chain link: flag seen by warp 0 -> warp 0 loads the
+// published block (double-buffered, one barrier) -> 16 FMAs per thread from
+// prefetched registers -> reduction -> Dinv (prefetched) -> store, fence, flag.
 template <typename C, bool LOWER>
 __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, int64_t lda, int n, const C* __restrict__ Dinv,
                                                    C* W, int64_t ldw, int nrhs, int* flags, unsigned* ticket, int epoch,
                                                    DeviceStatus* st) {
     using R = decltype(W[0].x);
-    __shared__ C xs[kB][kRc];            // a published block y_c
+    __shared__ C xs[2][kB][kRc];         // published blocks y_c (double buffer)
     __shared__ C part[4][kB][kRc];       // partial sums of the 4 column groups
-    __shared__ int s_t;
+    __shared__ C yb[kB][kRc];
+    __shared__ int s_t, s_abort;
     const int nb = (n + kB - 1) / kB;
-    if (threadIdx.x == 0) s_t = int(atomicAdd(ticket, 1u));
+    if (threadIdx.x == 0) {
+        s_t = int(atomicAdd(ticket, 1u));
+        s_abort = 0;
+    }
     __syncthreads();
     const int t = s_t;
     if (t >= nb) return;
     const int b = LOWER ? t : nb - 1 - t;
     const int r0 = b * kB, bs = min(kB, n - r0);
     const int r = threadIdx.x & 63, q = threadIdx.x >> 6;   // row in block, column group (16 cols)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // independent of the chain: own right-hand side (into yb), Dinv block, first T block
+    if (q == 0)
+#pragma unroll
+        for (int c = 0; c < kRc; c++)
+            yb[r][c] = (r < bs && c < nrhs) ? W[int64_t(c) * ldw + r0 + r] : cmake(R(0), R(0));
+    const C* D = Dinv + int64_t(b) * kB * kB;
+    C dv[16];
+#pragma unroll
+    for (int cc = 0; cc < 16; cc++) dv[cc] = (r < bs && q * 16 + cc < bs) ? D[(q * 16 + cc) * kB + r] : cmake(R(0), R(0));
     C acc[kRc];
 #pragma unroll
     for (int c = 0; c < kRc; c++) acc[c] = cmake(R(0), R(0));
-
-    // The 16 values of T this thread needs from the next dependency block are
-    // loaded before waiting on its flag (T does not depend on the chain), so
-    // the HBM latency overlaps the wait instead of serialising per element.
     const int ndep = LOWER ? b : nb - 1 - b;
     C lv[16];
     auto load_block = [&](int k) {
@@ -108,66 +122,62 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
             lv[cc] = (r < bs && q * 16 + cc < cs) ? col[int64_t(cc) * lda] : cmake(R(0), R(0));
     };
     if (ndep > 0) load_block(0);
+
     for (int k = 0; k < ndep; k++) {
         const int cb = LOWER ? k : nb - 1 - k;
         const int c0 = cb * kB, cs = min(kB, n - c0);
-        if (threadIdx.x == 0) {
-            volatile int* f = flags + cb;
-            long long t0 = clock64();
-            while (*f != epoch) {
-                if (clock64() - t0 > kWaitCycles) {
-                    if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
-                    break;
+        const int buf = k & 1;
+        if (warp == 0) {
+            if (lane == 0) {
+                volatile int* f = flags + cb;
+                volatile int* e = &st->err;
+                long long t0 = clock64();
+                while (*f != epoch) {
+                    if (*e) { s_abort = 1; break; }
+                    if (clock64() - t0 > kWaitCycles) {
+                        if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
+                        s_abort = 1;
+                        break;
+                    }
                 }
-                if (*(volatile int*)&st->err) break;
-                __nanosleep(64);
+            }
+            __syncwarp();
+            for (int idx = lane; idx < cs * nrhs; idx += 32) {
+                int rr = idx % cs, c = idx / cs;
+                xs[buf][rr][c] = __ldcg(&W[int64_t(c) * ldw + c0 + rr]);
             }
         }
         __syncthreads();
-        if (*(volatile int*)&st->err) return;
-        for (int idx = threadIdx.x; idx < cs * nrhs; idx += blockDim.x) {
-            int rr = idx % cs, c = idx / cs;
-            xs[rr][c] = __ldcg(&W[int64_t(c) * ldw + c0 + rr]);
-        }
-        __syncthreads();
+        if (s_abort) return;
         C cur[16];
 #pragma unroll
         for (int cc = 0; cc < 16; cc++) cur[cc] = lv[cc];
         if (k + 1 < ndep) load_block(k + 1);   // prefetch the next block's T values
-        if (r < bs) {
 #pragma unroll
-            for (int cc = 0; cc < 16; cc++) {
-                if (q * 16 + cc < cs) {
+        for (int cc = 0; cc < 16; cc++) {
 #pragma unroll
-                    for (int c = 0; c < kRc; c++)
-                        if (c < nrhs) acc[c] = cfms(acc[c], cur[cc], xs[q * 16 + cc][c]);
-                }
-            }
+            for (int c = 0; c < kRc; c++)
+                if (c < nrhs) acc[c] = cfms(acc[c], cur[cc], xs[buf][q * 16 + cc][c]);
         }
-        __syncthreads();
     }
     // y_pre = w_b + sum of the four partial sums
 #pragma unroll
     for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
     __syncthreads();
-    if (q == 0 && r < bs)
-        for (int c = 0; c < nrhs; c++) {
-            C s = W[int64_t(c) * ldw + r0 + r];
-            s = cadd(s, cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c])));
-            xs[r][c] = s;
-        }
+    if (q == 0)
+#pragma unroll
+        for (int c = 0; c < kRc; c++)
+            yb[r][c] = cadd(yb[r][c], cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c])));
     __syncthreads();
     // y = Dinv_b * y_pre
-    const C* D = Dinv + int64_t(b) * kB * kB;
 #pragma unroll
     for (int c = 0; c < kRc; c++) acc[c] = cmake(R(0), R(0));
-    if (r < bs)
-        for (int cc = q * 16; cc < q * 16 + 16 && cc < bs; cc++) {
-            C d = D[cc * kB + r];
 #pragma unroll
-            for (int c = 0; c < kRc; c++)
-                if (c < nrhs) acc[c] = cadd(acc[c], cmul(d, xs[cc][c]));
-        }
+    for (int cc = 0; cc < 16; cc++) {
+#pragma unroll
+        for (int c = 0; c < kRc; c++)
+            if (c < nrhs) acc[c] = cadd(acc[c], cmul(dv[cc], yb[q * 16 + cc][c]));
+    }
 #pragma unroll
     for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
     __syncthreads();

@@ -165,6 +165,7 @@ def test_mixed_pivoting_modes(gpu_lib, pivoting, engine):
     I = sim.solve()[:, 0]
     st = sim.stats()
     assert st["pivoting_used"] == (1 if pivoting == "partial" else 2)
+    assert 1 <= st["refine_iters"] <= 6   # complex64 factors good to ~1e-5: a few sweeps
     assert rel_norm(I, Ir) < MIXED_TOL
 
 
