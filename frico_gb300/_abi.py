@@ -79,6 +79,7 @@ PROTOTYPES = {
     "frico_gpu_get_factors": [P, P, I64, P],
     "frico_gpu_lump_currents": [P, I32, P, P, P],
     "frico_gpu_eval_fields": [P, I32, I64, P, P, P],
+    "frico_gpu_eval_fields_noalloc": [P, I32, I64, P, P, P],
     "frico_gpu_port_values": [P, I32, I32, P, C128, P, P],
     "frico_gpu_gain": [P, I32, D, D, I32, P],
     "frico_gpu_bistatic_rcs": [P, I32, D, P],

@@ -462,6 +462,37 @@ extern "C" int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t np
     return eval_fields_dev(ctx, col, npts, P, (double2*)E, (double2*)H);
 }
 
+// Device-pointer, allocation-free form of frico_gpu_eval_fields (no FRICO
+// counterpart). Every pointer is checked to be device memory of the context's
+// device before anything is launched, so a host pointer comes back as EINVAL.
+static int check_device_ptr(frico_gpu_ctx* ctx, const void* p, const char* what) {
+    if (!p) return FRICO_GPU_OK;
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, FRICO_GPU_EINVAL, std::string("eval_fields_noalloc: ") + what + " is not a device pointer");
+    }
+    if ((a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != ctx->device)
+        return set_err(ctx, FRICO_GPU_EINVAL,
+                       std::string("eval_fields_noalloc: ") + what + " is not device memory of the context's device");
+    return FRICO_GPU_OK;
+}
+
+extern "C" int frico_gpu_eval_fields_noalloc(frico_gpu_ctx* ctx, int32_t col, int64_t npts, const double* P_dev,
+                                             frico_c128* E_dev, frico_c128* H_dev) {
+    FRICO_CTX_CHECK(ctx);
+    int rc = check_col(ctx, col);
+    if (rc) return rc;
+    if (!ctx->solved) return set_err(ctx, FRICO_GPU_ESTATE, "eval_fields_noalloc: not solved");
+    if (npts <= 0 || !P_dev || (!E_dev && !H_dev))
+        return set_err(ctx, FRICO_GPU_EINVAL, "eval_fields_noalloc: need npts > 0, P_dev and E_dev or H_dev");
+    if ((rc = check_device_ptr(ctx, P_dev, "P_dev")) || (rc = check_device_ptr(ctx, E_dev, "E_dev")) ||
+        (rc = check_device_ptr(ctx, H_dev, "H_dev")))
+        return rc;
+    return eval_fields_noalloc(ctx, col, npts, P_dev, (double2*)E_dev, (double2*)H_dev);
+}
+
 extern "C" int frico_gpu_port_values(frico_gpu_ctx* ctx, int32_t col, int32_t n_itf, const int32_t* itf_tags,
                                      frico_c128 V0c, const double* signs, frico_port_values* out) {
     FRICO_CTX_CHECK(ctx);

@@ -192,5 +192,8 @@ int rhs_plane_wave(frico_gpu_ctx* ctx, double freq, int col, double theta, doubl
 int lump_currents(frico_gpu_ctx* ctx, int col);               // fields.cu
 int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_host,
                     double2* E_host, double2* H_host);        // fields.cu
+int eval_fields_noalloc(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_dev,
+                        double2* E_dev, double2* H_dev);      // fields.cu
+int64_t eval_fields_noalloc_max_points();                     // fields.cu
 
 }  // namespace frico

@@ -7,6 +7,9 @@
 //                           free-space kernel; H with exp(+jkR) in compat mode)
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <string>
+
 #include <algorithm>
 
 #include "common.cuh"
@@ -311,6 +314,92 @@ int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_h
             }
     }
     return FRICO_GPU_OK;
+}
+
+// ------------------------------------------------------------------ allocation-free field evaluation
+// Callers that cannot let the library allocate device memory in the middle of
+// their work use eval_fields_noalloc: an application whose own memory pool owns
+// (nearly) all of the device, or a post-processing loop that must not pay for
+// cudaMalloc's device-wide synchronisation on every new size. The points and the
+// fields are the caller's device buffers, and the per-chunk partial sums of
+// k_fields_part go to the fixed scratch array below, compiled into the library
+// (4 MiB: npts * chunks <= kNoAllocScratch / 6). Nothing in the scratch has to
+// start at zero: k_fields_part writes every (chunk, point) slot that
+// k_fields_reduce_split reads in the same call. The scratch is one array per
+// device, shared by every context: calls whose kernels overlap on the GPU (two
+// contexts, two streams) race on it.
+static const int64_t kNoAllocScratch = int64_t(1) << 18;   // double2 elements
+static __device__ __align__(256) double2 g_fields_scratch[kNoAllocScratch];
+
+static std::mutex g_scratch_mu;
+static const int kMaxDevices = 64;
+static double2* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_fields_scratch on ctx->device (the current device).
+// Looked up once per device, on the first call for that device.
+static int fields_scratch(frico_gpu_ctx* ctx, double2** out) {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (ctx->device < 0 || ctx->device >= kMaxDevices)
+        return set_err(ctx, FRICO_GPU_EINVAL, "eval_fields_noalloc: device ordinal out of range");
+    if (!g_scratch_ptr[ctx->device]) {
+        void* p = nullptr;
+        int rc = cuda_check(ctx, cudaGetSymbolAddress(&p, g_fields_scratch), "cudaGetSymbolAddress(fields scratch)");
+        if (rc) return rc;
+        g_scratch_ptr[ctx->device] = (double2*)p;
+    }
+    *out = g_scratch_ptr[ctx->device];
+    return FRICO_GPU_OK;
+}
+
+// E[3p + a] = sum over chunks of part[(c * npts + p) * 6 + a], H likewise (a + 3).
+__global__ void k_fields_reduce_split(int64_t npts, int nchunks, const double2* __restrict__ part,
+                                      double2* __restrict__ E, double2* __restrict__ H) {
+    int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (idx >= npts * 6) return;
+    double2 acc = make_double2(0, 0);
+    for (int c = 0; c < nchunks; c++) acc = cadd(acc, part[int64_t(c) * npts * 6 + idx]);
+    const int64_t p = idx / 6;
+    const int a = int(idx - p * 6);
+    if (a < 3) {
+        if (E) E[3 * p + a] = acc;
+    } else if (H) {
+        H[3 * p + a - 3] = acc;
+    }
+}
+
+int64_t eval_fields_noalloc_max_points() { return kNoAllocScratch / 6; }
+
+int eval_fields_noalloc(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_dev, double2* E_dev,
+                        double2* H_dev) {
+    if (npts > eval_fields_noalloc_max_points())
+        return set_err(ctx, FRICO_GPU_EINVAL,
+                       "eval_fields_noalloc: npts = " + std::to_string(npts) + " exceeds the fixed scratch limit of " +
+                           std::to_string(eval_fields_noalloc_max_points()) + " points");
+    if (ctx->lumped_col != col)
+        return set_err(ctx, FRICO_GPU_ESTATE,
+                       "eval_fields_noalloc: currents of this column are not lumped (call frico_gpu_lump_currents)");
+    int rc;
+    double2* part = nullptr;
+    if ((rc = fields_scratch(ctx, &part))) return rc;
+    const int64_t nt = ctx->nt;
+    const double omega = 2.0 * M_PI * ctx->freq;
+    const double k = omega * std::sqrt(FRICO_MU0 * FRICO_EPS0);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t pblocks = (npts + kFP - 1) / kFP;
+    // the same chunking as eval_fields_dev, capped by the scratch size
+    int64_t nchunks = std::max<int64_t>(1, (int64_t(8) * sms + pblocks - 1) / pblocks);
+    nchunks = std::min<int64_t>(nchunks, std::max<int64_t>(1, nt / 64));
+    nchunks = std::min<int64_t>(nchunks, kNoAllocScratch / (6 * npts));
+    const int64_t tpc = (nt + nchunks - 1) / nchunks;
+    nchunks = (nt + tpc - 1) / tpc;
+    k_fields_part<<<dim3(unsigned(pblocks), unsigned(nchunks)), kFP, 0, ctx->stream>>>(
+        npts, P_dev, nt, tpc, (const TriGeo*)ctx->trigeo.p, (const double2*)ctx->tri_aj.p,
+        (const double2*)ctx->tri_adivj.p, k, omega, ctx->opt.h_phase_mode == FRICO_HPHASE_PHYSICAL, part);
+    k_fields_reduce_split<<<unsigned((npts * 6 + 255) / 256), 256, 0, ctx->stream>>>(npts, int(nchunks), part, E_dev,
+                                                                                     H_dev);
+    count_launch(ctx, 2);
+    return cuda_check(ctx, cudaGetLastError(), "fields kernels (noalloc)");
 }
 
 }  // namespace frico

@@ -210,6 +210,24 @@ int frico_gpu_lump_currents(frico_gpu_ctx* ctx, int32_t col,
 int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t npts, const double* P,
                           frico_c128* E, frico_c128* H);
 
+/* Allocation-free form of frico_gpu_eval_fields; no counterpart in FRICO.
+ * It serves callers that cannot let the library allocate device memory while
+ * they run: an application whose own memory pool holds the device memory, or
+ * a post-processing loop that must not pay cudaMalloc's device-wide
+ * synchronisation. P_dev[3*npts] (points), E_dev[3*npts], H_dev[3*npts]
+ * (row-major rows of 3; either may be NULL) are device memory of the
+ * context's device; anything else is EINVAL. npts <= 43690: the partial sums
+ * use one fixed 4 MiB device array per device, and larger npts is EINVAL.
+ * The currents of `col` must already be lumped (frico_gpu_lump_currents),
+ * else ESTATE. The kernels are queued on the context stream and the call
+ * returns without waiting: E_dev/H_dev are valid once that stream reaches
+ * them. The scratch array is shared by every context on the device, so calls
+ * whose kernels overlap on the GPU race. The first call on each device looks
+ * up the scratch address (which may load the library's device code): make
+ * it before any stream capture. */
+int frico_gpu_eval_fields_noalloc(frico_gpu_ctx* ctx, int32_t col, int64_t npts,
+                                  const double* P_dev, frico_c128* E_dev, frico_c128* H_dev);
+
 /* compute_port_values for the delta gap on `itf_tags` (RHS column `col`). */
 int frico_gpu_port_values(frico_gpu_ctx* ctx, int32_t col, int32_t n_itf,
                           const int32_t* itf_tags, frico_c128 V0, const double* signs,
