@@ -60,33 +60,6 @@ def dist_env():
     return ws, rank, local
 
 
-class Dist:
-    def __init__(self, ws, rank, backend="gloo"):
-        self.ws, self.rank = ws, rank
-        self.pg = None
-        if ws > 1:
-            import torch.distributed as td
-            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-            td.init_process_group(backend, rank=rank, world_size=ws)
-            self.td = td
-
-    def barrier(self):
-        if self.ws > 1:
-            self.td.barrier()
-
-    def max(self, x: float) -> float:
-        if self.ws == 1:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
-        return float(t.item())
-
-    def close(self):
-        if self.ws > 1:
-            self.td.destroy_process_group()
-
-
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -197,7 +170,8 @@ def run_reference(args):
 # ------------------------------------------------------------------ GPU path
 def run_ours(args):
     ws, rank, local = dist_env()
-    dist = Dist(ws, rank)
+    from frico_gb300.replicas import ReplicaGroup
+    dist = ReplicaGroup(ws, rank)   # independent replicas: barrier + max of times only
     import ctypes as C
     import frico_gb300
     frico_gb300.build()
