@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gemm-engine", default="auto", choices=["auto", "simt", "tc"])
     ap.add_argument("--pivoting", default="auto", choices=["auto", "partial", "none"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "sweep"],
+                    help="sphere: one solve per step (headline); sweep: bowtie frequency sweep per step")
+    ap.add_argument("--sweep-n", type=int, default=3000, choices=[500, 1500, 3000])
+    ap.add_argument("--sweep-freqs", type=int, default=256)
+    ap.add_argument("--lanes", type=int, default=0, help="sweep lanes (0: chosen by the library)")
     return ap.parse_args()
 
 
@@ -165,6 +170,40 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (vector and tensor), nominal; no measured figure exists
+
+
+def stage_rooflines(stage, steps, n, nt, npts, iters, green_evals, precision, hbm, bf16):
+    """Per-stage achieved rate against its bound, with the work counts of the
+    stage table: fill = Green evaluations x 105 flops (FP64) and Z bytes
+    written; LU = 8/3 N^3; refinement = 16 N^2 bytes of FP64 Z per residual;
+    fields = Nobs Nt (30 + 90) flops (FP64)."""
+    per = {k: v / steps / 1000.0 for k, v in stage.items()}   # seconds per step
+    out = {}
+    if per["fill_ms"] > 0:
+        zb = (16.0 + (8.0 if precision == "mixed" else 0.0)) * n * n
+        fl = 105.0 * green_evals
+        out["fill"] = {"fp64_tflops": fl / per["fill_ms"] / 1e12,
+                       "fp64_frac_of_nominal": fl / per["fill_ms"] / 1e12 / FP64_NOMINAL_TFLOPS,
+                       "z_write_gbs": zb / per["fill_ms"] / 1e9, "hbm_frac": zb / per["fill_ms"] / 1e9 / hbm}
+    if per["factor_ms"] > 0:
+        t = (8.0 / 3.0) * n ** 3 / per["factor_ms"] / 1e12
+        out["lu"] = {"algorithmic_tflops": t,
+                     "frac": t * (3.0 if precision == "mixed" else 1.0) / (bf16 / 2.0 if precision == "mixed"
+                                                                            else FP64_NOMINAL_TFLOPS),
+                     "peak": "TF32 = measured bf16 / 2 (3xTF32 does 3 products)" if precision == "mixed"
+                     else "FP64 nominal"}
+    if per["refine_ms"] > 0 and iters and iters[-1] > 0:
+        gbs = 16.0 * n * n * iters[-1] / per["refine_ms"] / 1e9
+        out["refine"] = {"residual_gbs_equiv": gbs, "hbm_frac": gbs / hbm, "iters": iters[-1],
+                         "note": "whole refinement stage (residuals + triangular solves) against the residuals' Z reads"}
+    if per["fields_ms"] > 0:
+        fl = npts * nt * 120.0
+        out["fields"] = {"fp64_tflops": fl / per["fields_ms"] / 1e12,
+                         "fp64_frac_of_nominal": fl / per["fields_ms"] / 1e12 / FP64_NOMINAL_TFLOPS}
+    return out
 
 
 # ------------------------------------------------------------------ GPU path
@@ -290,6 +329,8 @@ def run_ours(args):
                        "precision": args.precision, "rhs": 1, "far_field_points": int(T.shape[0]),
                        "l2": "working set > L2 (Z 0.94 GB)", "replicas": ws},
             "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+            "stages_roofline": stage_rooflines(stage, args.steps, n, sim.nt, int(T.shape[0]), iters,
+                                               s1["green_evals"], args.precision, hbm, bf16),
             "refine_iters": iters[-1] if iters else 0,
             "pivoting_used": {1: "partial", 2: "none"}.get(s1["pivoting_used"], "?"),
             "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),
@@ -307,10 +348,83 @@ def run_ours(args):
     dist.close()
 
 
+# ------------------------------------------------------------------ sweep workload
+def run_sweep(args):
+    """Bowtie sweep: N ~ 500/1500/3000, 256 frequencies in [200, 800] MHz, 4 right-hand
+    sides per frequency (delta-gap feed + plane waves (0,0,theta), (45,0,theta),
+    (90,90,phi)), port values and E at 8 far-field points per RHS. One step = the
+    whole sweep through frico_gpu_sweep (host inputs, host outputs), so the
+    step time is also the end-to-end time."""
+    ws, rank, local = dist_env()
+    from frico_gb300.replicas import ReplicaGroup, shard
+    dist = ReplicaGroup(ws, rank)
+    import frico_gb300
+    frico_gb300.build()
+    from frico_gb300 import meshes
+    from frico_gb300.solver import DeltaGap, PlaneWave, Simulation
+    import torch
+    torch.cuda.set_device(local)
+    mesh = meshes.bowtie_preset(args.sweep_n)
+    all_freqs = meshes.sweep_frequencies(200e6, 800e6, args.sweep_freqs)
+    freqs = np.array(shard(list(all_freqs), rank, ws))   # weak scaling: each replica its own frequencies
+    d = np.pi / 180
+    pws = (PlaneWave(0.0, 0.0, 1.0, 0.0), PlaneWave(45 * d, 0.0, 1.0, 0.0), PlaneWave(90 * d, 90 * d, 0.0, 1.0))
+    feed = DeltaGap((meshes.FEED_TAG,), 1.0)
+    pts = meshes.sph2rect(10.0, np.linspace(0, 180, 8) * d, np.zeros(8))
+    sim = Simulation(mesh, precision=args.precision, device=local, gemm_engine=args.gemm_engine,
+                     pivoting=args.pivoting)
+    for _ in range(args.warmup):
+        out = sim.sweep(freqs, feed, pws, pts, lanes=args.lanes)
+    clocks = ClockSampler(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    reps = []
+    for _ in range(args.steps):
+        out = sim.sweep(freqs, feed, pws, pts, lanes=args.lanes)
+        reps.append(out["report"])
+    torch.cuda.synchronize()
+    sec = dist.max(time.perf_counter() - t0)
+    dist.barrier()
+    clk = clocks.stop()
+    nsys = len(all_freqs) * args.steps
+    value = nsys / sec
+    r = reps[-1]
+    nf = max(1, len(freqs))
+    n = sim.n
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sec / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64+c128" if args.precision == "mixed" else "c128",
+            "data": f"synthetic (seeded bowtie N={n})",
+            "config": {"workload": f"bowtie_sweep_N{n}_{len(all_freqs)}freq_4rhs", "n": n, "ntri": sim.nt,
+                       "precision": args.precision, "frequencies": int(len(all_freqs)), "rhs_per_frequency": 4,
+                       "far_field_points_per_rhs": 8, "lanes": r["lanes"], "autotuned": bool(r["autotuned"]),
+                       "solve_unit": "one frequency system (fill + LU + 4 RHS + port + fields)",
+                       "l2": "per-lane Z %.0f MB; lanes' Z together %s L2" % (
+                           16 * n * n / 1e6, ">" if 16 * n * n * r["lanes"] > 129e6 else "<"),
+                       "replicas": ws},
+            "stages_ms_per_frequency": {k: r[k] / nf for k in ("fill_ms", "rhs_ms", "factor_ms", "solve_ms",
+                                                                "refine_ms", "fields_ms")},
+            "max_refine_iters": r["max_refine_iters"], "partial_pivot_fallbacks": r["partial_pivot_fallbacks"],
+            "gpu_launches": int(sum(x["kernel_launches"] for x in reps)),
+            "e2e": {"value": value, "unit": "solves/s",
+                    "h2d_bytes_per_step": int(freqs.nbytes + pts.nbytes + 6 * 8 * 3),
+                    "d2h_bytes_per_step": int(nf * (4 * 8 * 3 * 16 + 88))},
+            "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    dist.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "sweep":
+        run_sweep(args)
     else:
         run_ours(args)
 

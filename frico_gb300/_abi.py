@@ -46,6 +46,15 @@ class PortValues(C.Structure):
                 ("gamma", C128), ("swr", C.c_double)]
 
 
+class SweepReport(C.Structure):
+    _fields_ = [("wall_ms", C.c_double), ("fill_ms", C.c_double), ("rhs_ms", C.c_double),
+                ("factor_ms", C.c_double), ("solve_ms", C.c_double), ("refine_ms", C.c_double),
+                ("lump_ms", C.c_double), ("fields_ms", C.c_double), ("lanes", C.c_int32),
+                ("autotuned", C.c_int32), ("nrhs", C.c_int32), ("max_refine_iters", C.c_int32),
+                ("max_refine_residual", C.c_double), ("partial_pivot_fallbacks", C.c_int32),
+                ("not_converged", C.c_int32), ("kernel_launches", C.c_int64)]
+
+
 class Stats(C.Structure):
     _fields_ = [("fill_ms", C.c_double), ("rhs_ms", C.c_double), ("factor_ms", C.c_double),
                 ("solve_ms", C.c_double), ("refine_ms", C.c_double), ("lump_ms", C.c_double),
@@ -80,6 +89,7 @@ PROTOTYPES = {
     "frico_gpu_lump_currents": [P, I32, P, P, P],
     "frico_gpu_eval_fields": [P, I32, I64, P, P, P],
     "frico_gpu_eval_fields_noalloc": [P, I32, I64, P, P, P],
+    "frico_gpu_sweep": [P, I32, P, I32, P, C128, P, I32, P, I64, P, I32, P, P, P, P],
     "frico_gpu_port_values": [P, I32, I32, P, C128, P, P],
     "frico_gpu_gain": [P, I32, D, D, I32, P],
     "frico_gpu_bistatic_rcs": [P, I32, D, P],

@@ -4,6 +4,9 @@
 // a kernel in fill.cu, lu.cu or fields.cu.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <set>
+
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -82,6 +85,18 @@ static int use_device(frico_gpu_ctx* ctx) { return cuda_check(ctx, cudaSetDevice
 
 using namespace frico;
 
+namespace frico {
+int device_once(frico_gpu_ctx* ctx, OnceKey key, int (*init)(frico_gpu_ctx*)) {
+    static std::mutex mu;
+    static std::set<std::pair<int, int>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({ctx->device, int(key)})) return FRICO_GPU_OK;
+    const int rc = init(ctx);
+    if (rc == FRICO_GPU_OK) done.insert({ctx->device, int(key)});
+    return rc;
+}
+}  // namespace frico
+
 #define FRICO_CTX_CHECK(ctx)                                 \
     do {                                                     \
         if (!(ctx)) return FRICO_GPU_EINVAL;                 \
@@ -118,6 +133,7 @@ extern "C" int frico_gpu_ctx_create(frico_gpu_ctx** out, int device, const frico
 
 extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
     if (!ctx) return FRICO_GPU_EINVAL;
+    destroy_lanes(ctx);
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     DevBuf* bufs[] = {&ctx->xyz,     &ctx->tri,      &ctx->trigeo,   &ctx->qp,        &ctx->qps,     &ctx->rwg_itm,
@@ -217,6 +233,9 @@ extern "C" int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* 
     ctx->nt = nt;
     ctx->n = n;
     ctx->h_rwg.assign(rwg, rwg + n);
+    ctx->h_xyz.assign(xyz, xyz + 3 * nv);
+    ctx->h_tri.assign(tri, tri + 3 * nt);
+    ctx->mesh_gen++;
     ctx->geo_degree = -1;
     ctx->z_valid = ctx->factored = ctx->solved = false;
     ctx->lumped_col = -1;

@@ -107,6 +107,13 @@ struct frico_gpu_ctx {
         rwg_vp, rwg_itf;
     frico::DevBuf tri_bf;         // [nt*3] basis index (+1, signed by side) per triangle slot
     std::vector<frico_rwg> h_rwg; // host copy (port values, interfaces)
+    std::vector<double> h_xyz;    // host copies of the mesh (sweep lanes are built from them)
+    std::vector<int64_t> h_tri;
+    int64_t mesh_gen = 0;         // bumped by every set_mesh
+
+    // frequency-sweep lanes: sub-contexts on the same device, one per concurrent frequency
+    std::vector<frico_gpu_ctx*> lanes;
+    int64_t lanes_mesh_gen = -1;
 
     // fill
     double freq = 0.0;
@@ -158,6 +165,13 @@ struct StageTimer {
     }
 };
 
+// One-time per-device setup (kernel attributes, constant tables): runs `init`
+// the first time (device, key) is seen in this process and returns its status;
+// a failed init runs again on the next call. Safe to call from several host
+// threads (each driving its own context).
+enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceKeys };
+int device_once(frico_gpu_ctx* ctx, OnceKey key, int (*init)(frico_gpu_ctx*));
+
 // Count one kernel launch on the context (reported as stats.kernel_launches).
 inline void count_launch(frico_gpu_ctx* ctx, int64_t k = 1) { ctx->stats.kernel_launches += k; }
 
@@ -195,5 +209,6 @@ int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_h
 int eval_fields_noalloc(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_dev,
                         double2* E_dev, double2* H_dev);      // fields.cu
 int64_t eval_fields_noalloc_max_points();                     // fields.cu
+void destroy_lanes(frico_gpu_ctx* ctx);                       // sweep.cu
 
 }  // namespace frico

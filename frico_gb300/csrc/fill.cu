@@ -448,23 +448,22 @@ __global__ void k_z64_to_z32(int64_t count, const double2* __restrict__ a, float
 }
 
 // ------------------------------------------------------------------ host side
-static bool g_tables_loaded = false;
+// The Dunavant tables live in constant memory, once per device.
+static int load_dunavant_tables(frico_gpu_ctx* ctx) {
+    int rc = cuda_check(ctx, cudaMemcpyToSymbol(c_orbits, frico_tables::kDunavantOrbits,
+                                                sizeof(frico_tables::kDunavantOrbits)),
+                        "copy Dunavant table");
+    if (rc) return rc;
+    return cuda_check(ctx, cudaMemcpyToSymbol(c_first, frico_tables::kDunavantFirst,
+                                              sizeof(frico_tables::kDunavantFirst)),
+                      "copy Dunavant offsets");
+}
 
 int build_quadrature(frico_gpu_ctx* ctx) {
     int degree = ctx->opt.degree;
     if (degree < 0 || degree > frico_tables::kDunavantMaxDegree)
         return set_err(ctx, FRICO_GPU_EINVAL, "Dunavant quadrature: degree too high");
-    if (!g_tables_loaded) {
-        int rc = cuda_check(ctx, cudaMemcpyToSymbol(c_orbits, frico_tables::kDunavantOrbits,
-                                                    sizeof(frico_tables::kDunavantOrbits)),
-                            "copy Dunavant table");
-        if (rc) return rc;
-        rc = cuda_check(ctx, cudaMemcpyToSymbol(c_first, frico_tables::kDunavantFirst,
-                                                sizeof(frico_tables::kDunavantFirst)),
-                        "copy Dunavant offsets");
-        if (rc) return rc;
-        g_tables_loaded = true;
-    }
+    if (int rc = device_once(ctx, kOnceDunavant, load_dunavant_tables)) return rc;
     int rule = degree == 0 ? 0 : degree - 1;
     int nq = frico_tables::kDunavantPoints[rule];
     int64_t nt = ctx->nt;

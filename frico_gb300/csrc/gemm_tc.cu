@@ -336,17 +336,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 static EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    static const EncodeTiledFn fn = [] {   // thread-safe one-time lookup
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
-        else
-            cudaGetLastError();
-    }
+            return (EncodeTiledFn)p;
+        cudaGetLastError();
+        return (EncodeTiledFn) nullptr;
+    }();
     return fn;
 }
 
@@ -393,13 +392,11 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     if (!make_map(&mah, Ah, M, KP) || !make_map(&mal, Al, M, KP) || !make_map(&mbh, Bh, n, KP) ||
         !make_map(&mbl, Bl, n, KP))
         return set_err(ctx, FRICO_GPU_ECUDA, "cuTensorMapEncodeTiled failed");
-    static bool attr_set = false;
-    if (!attr_set) {
-        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(tc::k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      tc::SMEM_BYTES), "tc smem attribute")))
-            return rc;
-        attr_set = true;
-    }
+    if ((rc = device_once(ctx, kOnceGemmTc, [](frico_gpu_ctx* c) {
+             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       tc::SMEM_BYTES), "tc smem attribute");
+         })))
+        return rc;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const int ntiles = ((M + tc::BM - 1) / tc::BM) * ((n + tc::BN - 1) / tc::BN);

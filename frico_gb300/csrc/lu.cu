@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <cstdio>
 
 #include "common.cuh"
@@ -856,14 +857,14 @@ int lu_factor_fp32(frico_gpu_ctx* ctx) { return lu_factor_impl<float>(ctx, (floa
 int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce) {
     if (ce <= cb) return FRICO_GPU_OK;
     const size_t smem = sizeof(float2) * (size_t(jb) * jb + 32 * jb);
-    static size_t set_for = 0;
-    if (smem > set_for) {
-        int rc = cuda_check(ctx, cudaFuncSetAttribute(k_trsm_lower_unit<float2>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)),
-                            "trsm smem attribute");
-        if (rc) return rc;
-        set_for = smem;
-    }
+    if (jb > 128) return set_err(ctx, FRICO_GPU_EINVAL, "trsm_lower_unit_f32: block wider than 128");
+    if (int rc = device_once(ctx, kOnceTrsmLower, [](frico_gpu_ctx* c) {
+            return cuda_check(c, cudaFuncSetAttribute(k_trsm_lower_unit<float2>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      int(sizeof(float2) * (128 * 128 + 32 * 128))),
+                              "trsm smem attribute");
+        }))
+        return rc;
     k_trsm_lower_unit<float2><<<(ce - cb + 31) / 32, 256, smem, ctx->stream>>>(A, lda, k0, jb, cb, ce);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_trsm_lower_unit");
@@ -948,10 +949,14 @@ int refine_solve(frico_gpu_ctx* ctx) {
         if ((rc = cuda_check(ctx, cudaStreamSynchronize(st), "refine sync"))) return rc;
         if ((rc = trsv_check(ctx))) return rc;
         rel = 0.0;
+        bool finite = true;
         for (int c = 0; c < nrhs; c++) {
             double bn = hn[nrhs + c] > 0 ? std::sqrt(hn[nrhs + c]) : 1.0;
-            rel = std::max(rel, std::sqrt(hn[c]) / bn);
+            const double v = std::sqrt(hn[c]) / bn;
+            finite = finite && std::isfinite(v);
+            rel = std::max(rel, v);
         }
+        if (!finite) rel = std::numeric_limits<double>::quiet_NaN();   // one bad column fails the solve
         src = Rr;
         if (!std::isfinite(rel)) { it++; break; }
         if (rel <= tol) { it++; break; }

@@ -308,17 +308,16 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     C* Uinv = (C*)ctx->panel_ws.p;
     C* Linv = Uinv + kNP * kNP;
     const size_t diag_smem = diag_lu_smem<C>();
-    const size_t right_smem = sizeof(C) * (kNP * kNP + 64 * kNP);
-    static bool attrs = false;
-    if (!attrs) {
-        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(k_diag_lu<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      int(diag_smem)), "diag smem")))
-            return rc;
-        if ((rc = cuda_check(ctx, cudaFuncSetAttribute(k_trsm_right<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      int(right_smem)), "trsm_right smem")))
-            return rc;
-        attrs = true;
-    }
+    if ((rc = device_once(ctx, kOnceNopivLu, [](frico_gpu_ctx* c) {
+             int r = cuda_check(c, cudaFuncSetAttribute(k_diag_lu<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        int(diag_lu_smem<float2>())), "diag smem");
+             if (r) return r;
+             return cuda_check(c, cudaFuncSetAttribute(k_trsm_right<float2>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       int(sizeof(float2) * (kNP * kNP + 64 * kNP))),
+                               "trsm_right smem");
+         })))
+        return rc;
     const bool tc = ctx->opt.gemm_engine != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
     if (ctx->opt.gemm_engine == FRICO_GEMM_TC && !tc)
         return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");

@@ -142,9 +142,11 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
                 }
             }
             __syncwarp();
-            for (int idx = lane; idx < cs * nrhs; idx += 32) {
-                int rr = idx % cs, c = idx / cs;
-                xs[buf][rr][c] = __ldcg(&W[int64_t(c) * ldw + c0 + rr]);
+            // rows past a short last block are zero: they meet zero T entries, and
+            // stale shared memory there could hold NaN (0 * NaN = NaN)
+            for (int idx = lane; idx < kB * nrhs; idx += 32) {
+                const int rr = idx & (kB - 1), c = idx >> 6;
+                xs[buf][rr][c] = rr < cs ? __ldcg(&W[int64_t(c) * ldw + c0 + rr]) : cmake(R(0), R(0));
             }
         }
         __syncthreads();

@@ -257,6 +257,39 @@ class Simulation:
         self.lib.frico_gpu_last_stats(self.ctx, C.byref(s))
         return {k: getattr(s, k) for k, _ in _abi.Stats._fields_}
 
+    def sweep(self, freqs, dgap: DeltaGap | None = None, plane_waves=(), points=None, lanes: int = 0,
+              currents: bool = False) -> dict:
+        """Batched frequency sweep (frico_gpu_sweep): per frequency, the delta gap
+        (if given) and then each plane wave as right-hand sides, port values of
+        the delta gap, optional currents and E at `points` for every RHS.
+        Frequencies run concurrently on `lanes` sub-contexts (0: chosen by the
+        library)."""
+        f = np.ascontiguousarray(freqs, np.float64).ravel()
+        nf = f.shape[0]
+        tags = np.asarray(dgap.interfaces if dgap is not None else (), np.int32)
+        v = complex(dgap.voltage) if dgap is not None else 0j
+        signs = None
+        if dgap is not None and self.delta_gap_signs is not None:
+            signs = np.ascontiguousarray(self.delta_gap_signs)
+        pw = np.array([[p.theta, p.phi, complex(p.Etheta).real, complex(p.Etheta).imag,
+                        complex(p.Ephi).real, complex(p.Ephi).imag] for p in plane_waves], np.float64).reshape(-1, 6)
+        nrhs = (1 if dgap is not None else 0) + pw.shape[0]
+        P = None if points is None else np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        npts = 0 if P is None else P.shape[0]
+        port = (_abi.PortValues * nf)() if dgap is not None else None
+        I = np.empty((nf, nrhs, self.n), np.complex128) if currents else None
+        E = np.empty((nf, nrhs, npts, 3), np.complex128) if npts else None
+        rep = _abi.SweepReport()
+        self._call("frico_gpu_sweep", nf, ptr(f), len(tags), ptr(tags), _abi.C128(v.real, v.imag), ptr(signs),
+                   pw.shape[0], ptr(pw), npts, ptr(P), int(lanes), port, ptr(I), ptr(E), C.byref(rep))
+        c = lambda z: complex(z.re, z.im)  # noqa: E731
+        ports = None
+        if port is not None:
+            ports = [{"voltage": c(p.voltage), "current": c(p.current), "power": c(p.power),
+                      "impedance": c(p.impedance), "gamma": c(p.gamma), "swr": p.swr} for p in port]
+        return {"freqs": f, "port": ports, "I": I, "E": E,
+                "report": {k: getattr(rep, k) for k, _ in _abi.SweepReport._fields_}}
+
     # -- composite, src/emw_solver.h:92-167
     def run_context(self, freq: float, src, download: bool = False):
         self.compute_matrix(freq)

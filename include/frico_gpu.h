@@ -228,6 +228,51 @@ int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t npts, const d
 int frico_gpu_eval_fields_noalloc(frico_gpu_ctx* ctx, int32_t col, int64_t npts,
                                   const double* P_dev, frico_c128* E_dev, frico_c128* H_dev);
 
+/* ---- batched frequency sweep ------------------------------------------
+ * FRICO's per-frequency loop (do_sweep, src/emw_ana_antenna.cpp:236-282 and
+ * src/emw_ana_bistatic_rcs.cpp:121-160, over the contexts init_sweep makes,
+ * src/emw_solver.cpp:460-468), run as independent concurrent lanes: each lane
+ * is a sub-context on the context's device with its own stream and buffers,
+ * driven by its own host thread, and takes the next frequency when it is done
+ * (fill -> right-hand sides -> factor + solve -> port values -> fields). Every
+ * frequency runs exactly the kernels of the single-frequency calls, so its
+ * results equal a frico_gpu_fill/solve/... sequence at that frequency.
+ *
+ * Right-hand sides per frequency (nrhs = (n_itf > 0) + n_pw), in this order:
+ * the delta gap on itf_tags (V0, signs as frico_gpu_rhs_delta_gap), then the
+ * plane waves pw[6*p .. 6*p+5] = {theta, phi, Re Etheta, Im Etheta, Re Ephi,
+ * Im Ephi}.
+ * Outputs (each optional): port_out[nfreq] (needs n_itf > 0);
+ * I_out[nfreq][nrhs][n] (currents, column-major per frequency);
+ * E_out[nfreq][nrhs][npts][3] (E at the npts points P[3*npts]).
+ * lanes: number of concurrent frequencies; 0 chooses it (by timing the first
+ * frequencies of a long sweep, else from N). The lane contexts are kept with
+ * ctx for later sweeps and freed by frico_gpu_ctx_destroy.
+ * Returns the first hard error (with the frequency in the message); a
+ * refinement that did not reach its tolerance at some frequency is counted in
+ * report->not_converged and the call returns FRICO_GPU_ENOCONV after finishing
+ * every frequency. */
+typedef struct frico_sweep_report {
+    double  wall_ms;             /* host wall-clock of the call                     */
+    double  fill_ms, rhs_ms, factor_ms, solve_ms, refine_ms, lump_ms, fields_ms;
+                                 /* device time per stage, summed over frequencies  */
+    int32_t lanes;               /* concurrent lanes of the bulk of the sweep       */
+    int32_t autotuned;           /* 1 when the lane count was chosen by timing      */
+    int32_t nrhs;
+    int32_t max_refine_iters;
+    double  max_refine_residual;
+    int32_t partial_pivot_fallbacks;  /* mixed path: frequencies factored with pivoting */
+    int32_t not_converged;       /* frequencies whose refinement missed its tolerance */
+    int64_t kernel_launches;     /* kernels launched by all lanes during the call   */
+} frico_sweep_report;
+
+int frico_gpu_sweep(frico_gpu_ctx* ctx, int32_t nfreq, const double* freqs,
+                    int32_t n_itf, const int32_t* itf_tags, frico_c128 V0, const double* signs,
+                    int32_t n_pw, const double* pw,
+                    int64_t npts, const double* P, int32_t lanes,
+                    frico_port_values* port_out, frico_c128* I_out, frico_c128* E_out,
+                    frico_sweep_report* report);
+
 /* compute_port_values for the delta gap on `itf_tags` (RHS column `col`). */
 int frico_gpu_port_values(frico_gpu_ctx* ctx, int32_t col, int32_t n_itf,
                           const int32_t* itf_tags, frico_c128 V0, const double* signs,
