@@ -50,8 +50,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gemm-engine", default="auto", choices=["auto", "simt", "tc"])
     ap.add_argument("--pivoting", default="auto", choices=["auto", "partial", "none"])
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "sweep"],
-                    help="sphere: one solve per step (headline); sweep: bowtie frequency sweep per step")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "sweep", "adjoint"],
+                    help="sphere: one solve per step (headline); sweep: bowtie frequency sweep per step; "
+                         "adjoint: bowtie gradients per step")
+    ap.add_argument("--validate", type=int, default=0,
+                    help="adjoint: check this many seeded random directions by central differences")
     ap.add_argument("--sweep-n", type=int, default=3000, choices=[500, 1500, 3000])
     ap.add_argument("--sweep-freqs", type=int, default=256)
     ap.add_argument("--lanes", type=int, default=0, help="sweep lanes (0: chosen by the library)")
@@ -408,6 +411,7 @@ def run_sweep(args):
             "stages_ms_per_frequency": {k: r[k] / nf for k in ("fill_ms", "rhs_ms", "factor_ms", "solve_ms",
                                                                 "refine_ms", "fields_ms")},
             "max_refine_iters": r["max_refine_iters"], "partial_pivot_fallbacks": r["partial_pivot_fallbacks"],
+            "fp64_fallbacks": r["fp64_fallbacks"],
             "gpu_launches": int(sum(x["kernel_launches"] for x in reps)),
             "e2e": {"value": value, "unit": "solves/s",
                     "h2d_bytes_per_step": int(freqs.nbytes + pts.nbytes + 6 * 8 * 3),
@@ -419,10 +423,106 @@ def run_sweep(args):
     dist.close()
 
 
+# ------------------------------------------------------------------ adjoint workload
+def run_adjoint(args):
+    """Bowtie N ~ 3000 at 500 MHz: gradients of Re Zin, Im Zin and |E(0, 0, 10 m)|^2
+    with respect to every vertex coordinate, the flare angle and the frequency.
+    One step = frico_gpu_adjoint (fill, LU, solve, transposed solve, reverse pass
+    over the fill) + the flare chain rule. --validate K compares K seeded random
+    directions with central differences (step 1e-6 wavelength) of the forward
+    path, outside the timed region."""
+    ws, rank, local = dist_env()
+    import frico_gb300
+    frico_gb300.build()
+    from frico_gb300 import meshes
+    from frico_gb300.solver import DeltaGap, Simulation
+    import torch
+    torch.cuda.set_device(local)
+    nx, ny = meshes.BOWTIE_PRESETS[args.sweep_n]
+    mesh = meshes.bowtie(nx, ny)
+    f0 = 500e6
+    feed = DeltaGap((meshes.FEED_TAG,), 1.0)
+    P = np.array([0.0, 0.0, 10.0])
+    tang = meshes.bowtie_flare_tangent(nx, ny)
+    sim = Simulation(mesh, precision=args.precision, device=local)
+
+    def step():
+        out = sim.adjoint(f0, feed, P)
+        G = np.stack([out["grad_zin_re"], out["grad_zin_im"], out["grad_e2"]])
+        return out, G, np.einsum("kvc,vc->k", G, tang)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out, G, dflare = step()
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    clk = clocks.stop()
+    # one forward solve, the unit a finite-difference gradient would repeat 2 (3 nv + 2) times
+    fwd = Simulation(mesh, precision=args.precision, device=local)
+    fwd.run_context(f0, feed)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(3):
+        fwd.run_context(f0, feed)
+        fwd.port_values(feed)
+        fwd.eval_fields(P[None, :])
+    torch.cuda.synchronize()
+    t_fwd = (time.perf_counter() - t1) / 3
+    fwd.close()
+    line = {"metric": "adjoint gradient evaluations/s", "value": args.steps / sec, "unit": "evals/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sec / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": f"synthetic (seeded bowtie N={sim.n})",
+            "config": {"workload": f"bowtie_adjoint_N{sim.n}_500MHz", "n": sim.n, "nv": int(mesh.nv),
+                       "parameters": 3 * int(mesh.nv) + 2, "objectives": ["Re Zin", "Im Zin", "|E(0,0,10)|^2"],
+                       "precision": args.precision},
+            "zin": [out["zin"].real, out["zin"].imag], "e2": out["e2"],
+            "d_dflare": list(map(float, dflare)),
+            "d_df": [out["dzin_df"].real, out["dzin_df"].imag, out["de2_df"]],
+            "forward_solve_ms": 1000 * t_fwd,
+            "finite_difference_equivalent_ms": 1000 * t_fwd * 2 * (3 * mesh.nv + 2),
+            "e2e": {"value": args.steps / sec, "unit": "evals/s", "h2d_bytes_per_step": 8 * 3,
+                    "d2h_bytes_per_step": 3 * 8 * 3 * int(mesh.nv)},
+            "clocks": clk}
+    if args.validate:
+        C0 = 1.0 / np.sqrt(1.256637061435917e-06 * 8.8541878188e-12)
+        h = 1e-6 * C0 / f0
+        rng = np.random.default_rng(20260104)
+
+        def J(verts):
+            m = meshes.bowtie(nx, ny)
+            m.vertices = verts
+            s2 = Simulation(m, precision="fp64", device=local)
+            s2.run_context(f0, feed)
+            z = s2.port_values(feed)["impedance"]
+            E, _ = s2.eval_fields(P[None, :])
+            s2.close()
+            return np.array([z.real, z.imag, float(np.sum(np.abs(E) ** 2))])
+
+        errs = []
+        scale = np.linalg.norm(G.reshape(3, -1), axis=1)
+        for _ in range(args.validate):
+            d = rng.standard_normal(mesh.vertices.shape)
+            d /= np.linalg.norm(d)
+            fd = (J(mesh.vertices + h * d) - J(mesh.vertices - h * d)) / (2 * h)
+            errs.append(np.abs(np.einsum("kvc,vc->k", G, d) - fd) / scale)
+        line["validation"] = {"directions": args.validate, "step_m": h,
+                              "max_err_over_grad_norm": list(map(float, np.max(errs, axis=0)))}
+    print(json.dumps(line), flush=True)
+    sim.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     elif args.workload == "sweep":
         run_sweep(args)
     else:

@@ -46,13 +46,19 @@ class PortValues(C.Structure):
                 ("gamma", C128), ("swr", C.c_double)]
 
 
+class AdjointResult(C.Structure):
+    _fields_ = [("zin", C128), ("e", C128 * 3), ("e2", C.c_double), ("dzin_re_df", C.c_double),
+                ("dzin_im_df", C.c_double), ("de2_df", C.c_double)]
+
+
 class SweepReport(C.Structure):
     _fields_ = [("wall_ms", C.c_double), ("fill_ms", C.c_double), ("rhs_ms", C.c_double),
                 ("factor_ms", C.c_double), ("solve_ms", C.c_double), ("refine_ms", C.c_double),
                 ("lump_ms", C.c_double), ("fields_ms", C.c_double), ("lanes", C.c_int32),
                 ("autotuned", C.c_int32), ("nrhs", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("max_refine_residual", C.c_double), ("partial_pivot_fallbacks", C.c_int32),
-                ("not_converged", C.c_int32), ("kernel_launches", C.c_int64)]
+                ("not_converged", C.c_int32), ("fp64_fallbacks", C.c_int32), ("reserved", C.c_int32),
+                ("kernel_launches", C.c_int64)]
 
 
 class Stats(C.Structure):
@@ -62,7 +68,7 @@ class Stats(C.Structure):
                 ("n", C.c_int64), ("ntri", C.c_int64), ("nrhs", C.c_int64), ("green_evals", C.c_int64),
                 ("kernel_launches", C.c_int64), ("gemm_launches", C.c_int64), ("gemm_ms", C.c_double),
                 ("gemm_flops", C.c_double), ("gemm_bytes", C.c_double), ("pivoting_used", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("precision_used", C.c_int32)]
 
 
 P = C.c_void_p
@@ -90,6 +96,9 @@ PROTOTYPES = {
     "frico_gpu_eval_fields": [P, I32, I64, P, P, P],
     "frico_gpu_eval_fields_noalloc": [P, I32, I64, P, P, P],
     "frico_gpu_sweep": [P, I32, P, I32, P, C128, P, I32, P, I64, P, I32, P, P, P, P],
+    "frico_gpu_adjoint": [P, D, I32, P, C128, P, P, I32, P, P, P, P],
+    "frico_gpu_eval_fields_multi": [P, I32, I32, I64, P, P, P],
+    "frico_gpu_rcs_points_multi": [P, I32, I32, D, I64, P, P, P],
     "frico_gpu_port_values": [P, I32, I32, P, C128, P, P],
     "frico_gpu_gain": [P, I32, D, D, I32, P],
     "frico_gpu_bistatic_rcs": [P, I32, D, P],

@@ -142,7 +142,8 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->z32,     &ctx->lu,       &ctx->ipiv,     &ctx->perm,      &ctx->panel_ws, &ctx->status,
                       &ctx->rhs,     &ctx->sol,      &ctx->rwork,    &ctx->rwork32,   &ctx->dwork32, &ctx->norms,
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
-                      &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws};
+                      &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws,   &ctx->lut,       &ctx->dinv_t,
+                      &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -351,7 +352,10 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
         ctx->stats.pivoting_used = partial ? FRICO_PIVOT_PARTIAL : FRICO_PIVOT_NONE;
         return r;
     };
-    if (!ctx->factored || ctx->factor_prec != ctx->opt.precision) {
+    // factors kept: same precision, or FP64 factors a mixed solve of this Z fell back to
+    const bool reuse = ctx->factored && (ctx->factor_prec == ctx->opt.precision ||
+                                         (mixed && ctx->factor_prec == FRICO_PREC_FP64));
+    if (!reuse) {
         if (!ctx->z_valid) return set_err(ctx, FRICO_GPU_ESTATE, "solve: no impedance matrix (call fill)");
         if (mixed) {
             rc = factor_mixed(piv == FRICO_PIVOT_PARTIAL);
@@ -379,7 +383,8 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
     ctx->stats.refine_iters = 0;
     ctx->stats.refine_residual = 0.0;
     const int64_t n = ctx->n;
-    if (mixed) {
+    bool fp64_solve = ctx->factor_prec == FRICO_PREC_FP64;
+    if (!fp64_solve) {
         {
             StageTimer tm(ctx, &ctx->stats.refine_ms);
             rc = refine_solve(ctx);
@@ -395,9 +400,27 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
             StageTimer tm(ctx, &ctx->stats.refine_ms);
             rc = refine_solve(ctx);
         }
+        if (rc == FRICO_GPU_ENOCONV && piv == FRICO_PIVOT_AUTO) {
+            // complex64 factors cannot refine this system: FP64 LU of the resident Z
+            StageTimer tm(ctx, &ctx->stats.factor_ms);
+            rc = lu_factor_fp64(ctx);
+            if (rc) return rc;
+            ctx->factor_prec = FRICO_PREC_FP64;
+            ctx->z_valid = false;
+            ctx->stats.pivoting_used = FRICO_PIVOT_PARTIAL;
+            if (ctx->info != 0) {
+                if (info) *info = ctx->info;
+                char buf[64];
+                snprintf(buf, sizeof buf, "ZGETRF singular matrix (info = %d)", ctx->info);
+                return set_err(ctx, FRICO_GPU_ESINGULAR, buf);
+            }
+            fp64_solve = true;
+        }
         ctx->stats.solve_ms = 0.0;
-    } else {
-        ctx->stats.refine_ms = 0.0;
+    }
+    ctx->stats.precision_used = fp64_solve ? FRICO_PREC_FP64 : FRICO_PREC_MIXED;
+    if (fp64_solve) {
+        if (!mixed) ctx->stats.refine_ms = 0.0;
         StageTimer tm(ctx, &ctx->stats.solve_ms);
         rc = ensure(ctx, ctx->sol, sizeof(double2) * n * ctx->nrhs);
         if (!rc)
@@ -635,6 +658,37 @@ extern "C" int frico_gpu_rcs_points(frico_gpu_ctx* ctx, int32_t col, double R, i
     int rc = frico_gpu_eval_fields(ctx, col, npts, P.data(), E.data(), nullptr);
     if (rc) return rc;
     for (int64_t i = 0; i < npts; i++) rcs_from_E(&E[3 * i], theta[i], phi[i], R, &out[2 * i], &out[2 * i + 1]);
+    return FRICO_GPU_OK;
+}
+
+extern "C" int frico_gpu_eval_fields_multi(frico_gpu_ctx* ctx, int32_t col0, int32_t ncols, int64_t npts,
+                                           const double* P, frico_c128* E, frico_c128* H) {
+    FRICO_CTX_CHECK(ctx);
+    if (!ctx->solved) return set_err(ctx, FRICO_GPU_ESTATE, "eval_fields_multi: not solved");
+    if (ncols <= 0 || col0 < 0 || col0 + ncols > ctx->nrhs)
+        return set_err(ctx, FRICO_GPU_EINVAL, "eval_fields_multi: column range outside [0, nrhs)");
+    if (npts <= 0 || !P || (!E && !H)) return set_err(ctx, FRICO_GPU_EINVAL, "eval_fields_multi: bad args");
+    StageTimer tm(ctx, &ctx->stats.fields_ms);
+    if (!E) {
+        std::vector<frico_c128> tmp(size_t(3) * ncols * npts);
+        return eval_fields_multi(ctx, col0, ncols, npts, P, (double2*)tmp.data(), (double2*)H);
+    }
+    return eval_fields_multi(ctx, col0, ncols, npts, P, (double2*)E, (double2*)H);
+}
+
+extern "C" int frico_gpu_rcs_points_multi(frico_gpu_ctx* ctx, int32_t col0, int32_t ncols, double R, int64_t npts,
+                                          const double* theta, const double* phi, double* out) {
+    FRICO_CTX_CHECK(ctx);
+    if (!out || !theta || !phi || npts <= 0) return set_err(ctx, FRICO_GPU_EINVAL, "rcs_points_multi: bad args");
+    std::vector<double> P(3 * npts);
+    for (int64_t i = 0; i < npts; i++) sph2rect(R, theta[i], phi[i], &P[3 * i]);
+    std::vector<frico_c128> E(size_t(3) * ncols * npts);
+    int rc = frico_gpu_eval_fields_multi(ctx, col0, ncols, npts, P.data(), E.data(), nullptr);
+    if (rc) return rc;
+    for (int64_t c = 0; c < ncols; c++)
+        for (int64_t i = 0; i < npts; i++)
+            rcs_from_E(&E[3 * (c * npts + i)], theta[i], phi[i], R, &out[2 * (c * npts + i)],
+                       &out[2 * (c * npts + i) + 1]);
     return FRICO_GPU_OK;
 }
 

@@ -122,7 +122,7 @@ struct frico_gpu_ctx {
 
     // factorisation / solve
     bool factored = false;
-    int factor_prec = -1;
+    int factor_prec = -1;         // precision of the resident factors (FP64 after a mixed fallback)
     int32_t info = 0;
     frico::DevBuf lu, ipiv, perm, panel_ws, status;
     int32_t nrhs = 0;
@@ -134,6 +134,10 @@ struct frico_gpu_ctx {
 
     // post-processing
     frico::DevBuf tri_aj, tri_adivj, tri_j, fld_pts, fld_part, fld_out;
+
+    // adjoint: transposed factors, their inverted diagonal blocks, workspaces
+    frico::DevBuf lut, dinv_t, adj_ws, adj_tab;
+    frico::DevBuf mlump, mfld;    // multi-column lumped currents and field partial sums
     int32_t lumped_col = -1;
 
     frico_gpu_stats stats{};
@@ -210,5 +214,11 @@ int eval_fields_noalloc(frico_gpu_ctx* ctx, int col, int64_t npts, const double*
                         double2* E_dev, double2* H_dev);      // fields.cu
 int64_t eval_fields_noalloc_max_points();                     // fields.cu
 void destroy_lanes(frico_gpu_ctx* ctx);                       // sweep.cu
+int eval_fields_multi(frico_gpu_ctx* ctx, int col0, int ncols, int64_t npts, const double* P_host,
+                      double2* E_host, double2* H_host);     // fields_multi.cu
+int trsv_solve_with_fp64(frico_gpu_ctx* ctx, const double2* LU, DevBuf& dinv, double2* W, int nrhs,
+                         int64_t ldw);                        // trsv.cu
+int trsv_solve_with_fp32(frico_gpu_ctx* ctx, const float2* LU, DevBuf& dinv, float2* W, int nrhs,
+                         int64_t ldw);                        // trsv.cu
 
 }  // namespace frico

@@ -139,9 +139,12 @@ int run_frequency(frico_gpu_ctx* lane, const SweepArgs& a, int fi, Tally& t) {
     r.fields_ms += fields_ms;
     r.max_refine_iters = std::max(r.max_refine_iters, s.refine_iters);
     r.max_refine_residual = std::max(r.max_refine_residual, s.refine_residual);
-    if (lane->opt.precision == FRICO_PREC_MIXED && lane->opt.pivoting != FRICO_PIVOT_PARTIAL &&
-        s.pivoting_used == FRICO_PIVOT_PARTIAL)
-        r.partial_pivot_fallbacks++;
+    if (lane->opt.precision == FRICO_PREC_MIXED) {
+        if (s.precision_used == FRICO_PREC_FP64)
+            r.fp64_fallbacks++;
+        else if (lane->opt.pivoting != FRICO_PIVOT_PARTIAL && s.pivoting_used == FRICO_PIVOT_PARTIAL)
+            r.partial_pivot_fallbacks++;
+    }
     if (noconv) r.not_converged++;
     r.kernel_launches += s.kernel_launches - launches0;
     return FRICO_GPU_OK;

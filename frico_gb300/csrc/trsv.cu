@@ -253,6 +253,16 @@ int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     return trsv_solve<float2>(ctx, (const float2*)ctx->z32.p, ctx->dinv, ctx->trsv_flags, W, nrhs, ldw);
 }
 
+// The same chained solves with caller-supplied factors and inverted diagonal
+// blocks (first nb blocks for the lower pass, next nb for the upper pass); the
+// transposed solves of the adjoint use them on transposed factors.
+int trsv_solve_with_fp64(frico_gpu_ctx* ctx, const double2* LU, DevBuf& dinv, double2* W, int nrhs, int64_t ldw) {
+    return trsv_solve<double2>(ctx, LU, dinv, ctx->trsv_flags, W, nrhs, ldw);
+}
+int trsv_solve_with_fp32(frico_gpu_ctx* ctx, const float2* LU, DevBuf& dinv, float2* W, int nrhs, int64_t ldw) {
+    return trsv_solve<float2>(ctx, LU, dinv, ctx->trsv_flags, W, nrhs, ldw);
+}
+
 // Checks the device status word after a solve (host-synchronous).
 int trsv_check(frico_gpu_ctx* ctx) {
     DeviceStatus hs;

@@ -173,6 +173,17 @@ def bowtie(nx: int, ny: int, arm: float = 0.25, flare_deg: float = 60.0, gap: fl
                    np.array(feed, np.int64), np.full(len(feed), FEED_TAG, np.int32), (FEED_TAG,))
 
 
+def bowtie_flare_tangent(nx: int, ny: int, flare_deg: float = 60.0, **kw) -> np.ndarray:
+    """d(vertices)/d(flare angle in radians) of bowtie(nx, ny, flare_deg=...): the
+    vertices depend on the flare only through tan(flare/2), linearly, so a
+    central difference in the angle (h = 1e-6 rad) is accurate to ~1e-9."""
+    h = 1e-6
+    hd = np.degrees(h)
+    vp = bowtie(nx, ny, flare_deg=flare_deg + hd, **kw).vertices
+    vm = bowtie(nx, ny, flare_deg=flare_deg - hd, **kw).vertices
+    return (vp - vm) / (2 * h)
+
+
 def bowtie_preset(n_target: int, **kw) -> TriMesh:
     nx, ny = BOWTIE_PRESETS[n_target]
     return bowtie(nx, ny, **kw)

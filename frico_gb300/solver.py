@@ -252,6 +252,39 @@ class Simulation:
         self._call("frico_gpu_rcs_points", col, float(R), th.shape[0], ptr(th), ptr(ph), ptr(out))
         return out
 
+    def eval_fields_multi(self, points, col0: int = 0, ncols: int | None = None, want_h: bool = True):
+        """E, H for columns [col0, col0 + ncols): arrays (ncols, npts, 3)."""
+        Pt = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        nc = self.nrhs - col0 if ncols is None else ncols
+        E = np.empty((nc, Pt.shape[0], 3), np.complex128)
+        H = np.empty((nc, Pt.shape[0], 3), np.complex128) if want_h else None
+        self._call("frico_gpu_eval_fields_multi", col0, nc, Pt.shape[0], ptr(Pt), ptr(E), ptr(H))
+        return E, H
+
+    def rcs_points_multi(self, R: float, theta, phi, col0: int = 0, ncols: int | None = None) -> np.ndarray:
+        """sigma_VV, sigma_HH for columns [col0, col0 + ncols) at the same points: (ncols, npts, 2)."""
+        th = np.ascontiguousarray(theta, np.float64)
+        ph = np.ascontiguousarray(phi, np.float64)
+        nc = self.nrhs - col0 if ncols is None else ncols
+        out = np.empty((nc, th.shape[0], 2))
+        self._call("frico_gpu_rcs_points_multi", col0, nc, float(R), th.shape[0], ptr(th), ptr(ph), ptr(out))
+        return out
+
+    def monostatic_rcs(self, freq: float, theta, phi, Etheta=1.0, Ephi=1.0, R: float = 10.0) -> np.ndarray:
+        """Monostatic RCS (FRICO's -m, left unimplemented there: src/main.cpp:92-93,
+        src/emw_postpro_rcs.cpp:63-97): one plane-wave right-hand side per
+        incidence direction (theta[c], phi[c]) in a single multi-RHS solve, and
+        sigma_VV, sigma_HH (bistatic_RCS_unit_Ei) observed back along that
+        direction at distance R. Returns (len(theta), 2)."""
+        th = np.atleast_1d(np.asarray(theta, np.float64))
+        ph = np.broadcast_to(np.asarray(phi, np.float64), th.shape).copy()
+        self.compute_matrix(freq)
+        self.set_nrhs(th.shape[0])
+        for c in range(th.shape[0]):
+            self.update_rhs(freq, PlaneWave(float(th[c]), float(ph[c]), Etheta, Ephi), c)
+        self.solve(download=False)
+        return np.stack([self.rcs_points(R, th[c:c + 1], ph[c:c + 1], col=c)[0] for c in range(th.shape[0])])
+
     def stats(self) -> dict:
         s = _abi.Stats()
         self.lib.frico_gpu_last_stats(self.ctx, C.byref(s))
@@ -289,6 +322,35 @@ class Simulation:
                       "impedance": c(p.impedance), "gamma": c(p.gamma), "swr": p.swr} for p in port]
         return {"freqs": f, "port": ports, "I": I, "E": E,
                 "report": {k: getattr(rep, k) for k, _ in _abi.SweepReport._fields_}}
+
+    def adjoint(self, freq: float, dgap: DeltaGap, P_obs, edge_length: str = "xy") -> dict:
+        """Gradients of Re Zin, Im Zin and |E(P_obs)|^2 with respect to every vertex
+        coordinate of the input mesh ((nv, 3) arrays in the mesh's own vertex
+        numbering; unused vertices get 0) and the frequency (frico_gpu_adjoint).
+        Runs the fill and solve at `freq` on this simulation's context."""
+        tags = np.asarray(dgap.interfaces, np.int32)
+        v = complex(dgap.voltage)
+        signs = None if self.delta_gap_signs is None else np.ascontiguousarray(self.delta_gap_signs)
+        P = np.ascontiguousarray(P_obs, np.float64).reshape(3)
+        nvc = self.fs.vertices.shape[0]
+        g = [np.zeros((nvc, 3)) for _ in range(3)]
+        res = _abi.AdjointResult()
+        mode = _abi.EDGE_LENGTH_XY if edge_length == "xy" else _abi.EDGE_LENGTH_TRUE
+        self._call("frico_gpu_adjoint", float(freq), len(tags), ptr(tags), _abi.C128(v.real, v.imag), ptr(signs),
+                   ptr(P), mode, ptr(g[0]), ptr(g[1]), ptr(g[2]), C.byref(res))
+        self.freq = freq
+        self.nrhs = 1
+        # compacted vertex k is the k-th used vertex of the input mesh, in input order
+        used = np.unique(np.asarray(self.mesh.triangles).ravel())
+        full = []
+        for a in g:
+            f = np.zeros((self.mesh.nv, 3))
+            f[used] = a
+            full.append(f)
+        c = lambda z: complex(z.re, z.im)  # noqa: E731
+        return {"zin": c(res.zin), "E": np.array([c(res.e[a]) for a in range(3)]), "e2": res.e2,
+                "grad_zin_re": full[0], "grad_zin_im": full[1], "grad_e2": full[2],
+                "dzin_df": complex(res.dzin_re_df, res.dzin_im_df), "de2_df": res.de2_df}
 
     # -- composite, src/emw_solver.h:92-167
     def run_context(self, freq: float, src, download: bool = False):

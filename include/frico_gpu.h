@@ -121,7 +121,7 @@ typedef struct frico_gpu_stats {
     double  gemm_flops;          /* their algorithmic real flops (8 m n k)  */
     double  gemm_bytes;          /* their algorithmic bytes: C read+write + L, U reads */
     int32_t pivoting_used;       /* FRICO_PIVOT_PARTIAL / _NONE of the last factorisation */
-    int32_t reserved;
+    int32_t precision_used;      /* FRICO_PREC_FP64 when a mixed solve fell back to FP64 LU */
 } frico_gpu_stats;
 
 typedef struct frico_gpu_ctx frico_gpu_ctx;
@@ -195,7 +195,10 @@ int frico_gpu_get_rhs(frico_gpu_ctx* ctx, frico_c128* V, int64_t ldv);
  * pivoting by max |re|+|im|) and solve Z I = V for all nrhs columns.
  * *info: 0, or k>0 for an exactly-zero pivot in column k (1-based), as zgetrf.
  * I_out (n x nrhs, ld ldi) optional. With FRICO_PREC_MIXED the factorisation
- * is complex64 and the currents are refined against the FP64 Z. */
+ * is complex64 and the currents are refined against the FP64 Z; with
+ * FRICO_PIVOT_AUTO a system the complex64 factors cannot refine (too
+ * ill-conditioned, e.g. an electrically small antenna) is re-solved with the
+ * FP64 LU (stats.precision_used = FRICO_PREC_FP64). */
 int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ldi, int32_t* info);
 /* Download the LU factors (FP64 path: LAPACK layout) and 1-based ipiv. */
 int frico_gpu_get_factors(frico_gpu_ctx* ctx, frico_c128* LU, int64_t ld, int32_t* ipiv);
@@ -263,6 +266,8 @@ typedef struct frico_sweep_report {
     double  max_refine_residual;
     int32_t partial_pivot_fallbacks;  /* mixed path: frequencies factored with pivoting */
     int32_t not_converged;       /* frequencies whose refinement missed its tolerance */
+    int32_t fp64_fallbacks;      /* mixed path: frequencies solved by the FP64 LU   */
+    int32_t reserved;
     int64_t kernel_launches;     /* kernels launched by all lanes during the call   */
 } frico_sweep_report;
 
@@ -272,6 +277,41 @@ int frico_gpu_sweep(frico_gpu_ctx* ctx, int32_t nfreq, const double* freqs,
                     int64_t npts, const double* P, int32_t lanes,
                     frico_port_values* port_out, frico_c128* I_out, frico_c128* E_out,
                     frico_sweep_report* report);
+
+/* ---- adjoint sensitivities ---------------------------------------------
+ * No counterpart in FRICO (it computes no derivatives): the reverse mode of its
+ * antenna pipeline at one frequency, for the fill it runs by default (degree-1
+ * quadrature with the sub-triangle split, src/emw_solver.cpp:45-142). Runs
+ * fill -> delta-gap RHS -> solve at `freq` (the context's precision), then one
+ * transposed solve with the same factors for the two adjoint vectors, and a
+ * reverse pass over the fill on the GPU. Outputs the gradients of Re Zin,
+ * Im Zin (Zin = V0 / sum_feed l_i s_i I_i, as compute_port_values) and of
+ * |E(P_obs)|^2 (eval_fields' E) with respect to every vertex coordinate of
+ * the mesh given to frico_gpu_set_mesh (grad_*[3*nv], each may be NULL), and
+ * with respect to the frequency (in *out). edge_length_mode must be the one
+ * the RWG lengths were made with (FRICO_EDGE_LENGTH_XY as FRICO does). */
+typedef struct frico_adjoint_result {
+    frico_c128 zin;              /* input impedance                         */
+    frico_c128 e[3];             /* E(P_obs)                                */
+    double     e2;               /* |E(P_obs)|^2                            */
+    double     dzin_re_df, dzin_im_df, de2_df;   /* per Hz                */
+} frico_adjoint_result;
+
+int frico_gpu_adjoint(frico_gpu_ctx* ctx, double freq, int32_t n_itf, const int32_t* itf_tags,
+                      frico_c128 V0, const double* signs, const double* P_obs,
+                      int32_t edge_length_mode,
+                      double* grad_zin_re, double* grad_zin_im, double* grad_e2,
+                      frico_adjoint_result* out);
+
+/* eval_fields for RHS columns [col0, col0 + ncols) at the same npts points:
+ * E[ncols][npts][3], H[ncols][npts][3] (either may be NULL). One pass over
+ * (point, triangle) pairs serves every column (the Green function is shared). */
+int frico_gpu_eval_fields_multi(frico_gpu_ctx* ctx, int32_t col0, int32_t ncols, int64_t npts,
+                                const double* P, frico_c128* E, frico_c128* H);
+/* bistatic_RCS_unit_Ei at sph2rect(R, theta[i], phi[i]) for every column:
+ * out[ncols][npts][2] = {sigma_VV, sigma_HH}. */
+int frico_gpu_rcs_points_multi(frico_gpu_ctx* ctx, int32_t col0, int32_t ncols, double R, int64_t npts,
+                               const double* theta, const double* phi, double* out);
 
 /* compute_port_values for the delta gap on `itf_tags` (RHS column `col`). */
 int frico_gpu_port_values(frico_gpu_ctx* ctx, int32_t col, int32_t n_itf,

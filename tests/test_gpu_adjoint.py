@@ -1,0 +1,101 @@
+"""Adjoint sensitivities (frico_gpu_adjoint) against central finite differences
+of the forward pipeline: gradients of Re Zin, Im Zin and |E(0, 0, 10 m)|^2 of
+the bowtie with respect to vertex coordinates (seeded random directions, step
+1e-6 wavelength), the frequency and the flare angle."""
+import numpy as np
+import pytest
+
+from frico_gb300 import meshes
+from frico_gb300.solver import DeltaGap, Simulation
+
+C0 = 1.0 / np.sqrt(1.256637061435917e-06 * 8.8541878188e-12)
+FEED = DeltaGap((meshes.FEED_TAG,), 1.0)
+P_OBS = np.array([0.0, 0.0, 10.0])
+NX, NY = 13, 7          # N ~ 500
+FREQ = 500e6
+
+
+def _forward(mesh, f, precision="fp64"):
+    sim = Simulation(mesh, precision=precision)
+    sim.run_context(f, FEED)
+    zin = sim.port_values(FEED)["impedance"]
+    E, _ = sim.eval_fields(P_OBS[None, :])
+    sim.close()
+    return np.array([zin.real, zin.imag, float(np.sum(np.abs(E) ** 2))])
+
+
+def _moved(mesh, dv):
+    m = meshes.bowtie(NX, NY)
+    m.vertices = mesh.vertices + dv
+    return m
+
+
+@pytest.fixture(scope="module")
+def adj():
+    mesh = meshes.bowtie(NX, NY)
+    sim = Simulation(mesh, precision="fp64")
+    out = sim.adjoint(FREQ, FEED, P_OBS)
+    sim.close()
+    return mesh, out
+
+
+@pytest.mark.gpu
+def test_adjoint_values_match_forward(gpu_lib, adj):
+    mesh, out = adj
+    ref = _forward(mesh, FREQ)
+    assert abs(out["zin"].real - ref[0]) <= 1e-10 * abs(out["zin"])
+    assert abs(out["zin"].imag - ref[1]) <= 1e-10 * abs(out["zin"])
+    assert abs(out["e2"] - ref[2]) <= 1e-9 * ref[2]
+
+
+@pytest.mark.gpu
+def test_adjoint_vertex_gradients_match_central_differences(gpu_lib, adj):
+    mesh, out = adj
+    G = np.stack([out["grad_zin_re"], out["grad_zin_im"], out["grad_e2"]])   # (3, nv, 3)
+    h = 1e-6 * C0 / FREQ
+    rng = np.random.default_rng(4242)
+    for _ in range(6):
+        d = rng.standard_normal(mesh.vertices.shape)
+        d /= np.linalg.norm(d)
+        fd = (_forward(_moved(mesh, h * d), FREQ) - _forward(_moved(mesh, -h * d), FREQ)) / (2 * h)
+        ad = np.einsum("kvc,vc->k", G, d)
+        scale = np.linalg.norm(G.reshape(3, -1), axis=1)   # |grad| (d is a unit vector)
+        assert np.all(np.abs(ad - fd) <= 2e-5 * scale), (ad, fd, scale)
+
+
+@pytest.mark.gpu
+def test_adjoint_frequency_and_flare_derivatives(gpu_lib, adj):
+    mesh, out = adj
+    hf = 1e-6 * FREQ
+    fd = (_forward(mesh, FREQ + hf) - _forward(mesh, FREQ - hf)) / (2 * hf)
+    ad = np.array([out["dzin_df"].real, out["dzin_df"].imag, out["de2_df"]])
+    assert np.all(np.abs(ad - fd) <= 1e-5 * np.abs(fd) + 1e-12 * np.abs(_forward(mesh, FREQ)) / FREQ), (ad, fd)
+    # flare angle: chain rule through the mesh generator
+    tang = meshes.bowtie_flare_tangent(NX, NY)
+    G = np.stack([out["grad_zin_re"], out["grad_zin_im"], out["grad_e2"]])
+    ad_fl = np.einsum("kvc,vc->k", G, tang)
+    hd = np.degrees(1e-5)
+    fd_fl = (_forward(meshes.bowtie(NX, NY, flare_deg=60 + hd), FREQ)
+             - _forward(meshes.bowtie(NX, NY, flare_deg=60 - hd), FREQ)) / (2e-5)
+    assert np.all(np.abs(ad_fl - fd_fl) <= 1e-4 * np.abs(fd_fl)), (ad_fl, fd_fl)
+
+
+@pytest.mark.gpu
+def test_adjoint_mixed_matches_fp64(gpu_lib, adj):
+    mesh, out = adj
+    sim = Simulation(mesh, precision="mixed")
+    mx = sim.adjoint(FREQ, FEED, P_OBS)
+    sim.close()
+    for k in ("grad_zin_re", "grad_zin_im", "grad_e2"):
+        assert np.linalg.norm(mx[k] - out[k]) <= 1e-6 * np.linalg.norm(out[k])
+    assert abs(mx["zin"] - out["zin"]) <= 1e-8 * abs(out["zin"])
+
+
+@pytest.mark.gpu
+def test_adjoint_rejects_unsupported_fill(gpu_lib):
+    from frico_gb300._abi import FricoError
+    sim = Simulation(meshes.bowtie(NX, NY), degree=2)
+    with pytest.raises(FricoError) as e:
+        sim.adjoint(FREQ, FEED, P_OBS)
+    assert e.value.code == -1
+    sim.close()

@@ -268,3 +268,23 @@ def test_error_paths(gpu_lib, strip):
     with pytest.raises(FricoError) as e:
         sim.compute_matrix(-1.0)
     assert e.value.code == -1
+
+
+def test_mixed_falls_back_to_fp64_lu_when_refinement_cannot(gpu_lib, strip):
+    """When neither complex64 factorisation refines to the tolerance (here forced
+    by allowing a single refinement sweep), the mixed solve returns the FP64 LU
+    solution of the same Z and keeps those factors for further solves."""
+    f = 300e6
+    fp = Simulation(strip, precision="fp64")
+    fp.run_context(f, DeltaGap((meshes.FEED_TAG,), 1.0))
+    Ir = fp.solve()
+    mx = Simulation(strip, precision="mixed", max_refine_iters=1)
+    mx.compute_matrix(f)
+    mx.set_nrhs(1)
+    mx.update_rhs(f, DeltaGap((meshes.FEED_TAG,), 1.0))
+    I = mx.solve()
+    st = mx.stats()
+    assert st["precision_used"] == 0 and st["pivoting_used"] == 1
+    np.testing.assert_array_equal(I, Ir)
+    I2 = mx.solve()                       # the FP64 factors stay for further right-hand sides
+    np.testing.assert_array_equal(I2, Ir)
