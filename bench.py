@@ -50,8 +50,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gemm-engine", default="auto", choices=["auto", "simt", "tc"])
     ap.add_argument("--pivoting", default="auto", choices=["auto", "partial", "none"])
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "sweep", "adjoint"],
-                    help="sphere: one solve per step (headline); sweep: bowtie frequency sweep per step; "
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "sphere64", "sweep", "adjoint"],
+                    help="sphere: one solve per step (headline); sphere64: level-5 sphere, 64 incidences, "
+                         "181 x 361 bistatic grid; sweep: bowtie frequency sweep per step; "
                          "adjoint: bowtie gradients per step")
     ap.add_argument("--validate", type=int, default=0,
                     help="adjoint: check this many seeded random directions by central differences")
@@ -411,7 +412,7 @@ def run_sweep(args):
             "stages_ms_per_frequency": {k: r[k] / nf for k in ("fill_ms", "rhs_ms", "factor_ms", "solve_ms",
                                                                 "refine_ms", "fields_ms")},
             "max_refine_iters": r["max_refine_iters"], "partial_pivot_fallbacks": r["partial_pivot_fallbacks"],
-            "fp64_fallbacks": r["fp64_fallbacks"],
+            "fp64_fallbacks": r["fp64_fallbacks"], "fp64_direct": r["fp64_direct"],
             "gpu_launches": int(sum(x["kernel_launches"] for x in reps)),
             "e2e": {"value": value, "unit": "solves/s",
                     "h2d_bytes_per_step": int(freqs.nbytes + pts.nbytes + 6 * 8 * 3),
@@ -517,12 +518,87 @@ def run_adjoint(args):
     sim.close()
 
 
+# ------------------------------------------------------------------ many-incidence workload
+def run_sphere64(args):
+    """Sphere level 5 (N = 30 720) at 900 MHz, 64 plane waves theta_i = i 180/63 deg,
+    phi = 0, polarisation alternating theta / phi, sigma_VV and sigma_HH of every
+    incidence on the 181 x 361 (theta x phi) grid at R = 10 m (65 341 points).
+    One step = fill + one 64-RHS solve + the multi-column field pass, timed on
+    the host clock around device-synchronised calls."""
+    ws, rank, local = dist_env()
+    import frico_gb300
+    frico_gb300.build()
+    from frico_gb300 import meshes
+    from frico_gb300.solver import PlaneWave, Simulation
+    import torch
+    torch.cuda.set_device(local)
+    level = args.level if args.level != 4 else 5
+    mesh = meshes.icosphere(level)
+    f0 = 900e6 if level == 5 else 450e6
+    nrhs = 64
+    th_in = np.arange(nrhs) * np.pi / (nrhs - 1)
+    pws = [PlaneWave(float(t), 0.0, 1.0 if i % 2 == 0 else 0.0, 0.0 if i % 2 == 0 else 1.0)
+           for i, t in enumerate(th_in)]
+    th = np.radians(np.arange(181.0))
+    ph = np.radians(np.arange(361.0))
+    T, Pg = np.meshgrid(th, ph, indexing="ij")
+    T, Pg = T.ravel(), Pg.ravel()
+    sim = Simulation(mesh, precision=args.precision, device=local, gemm_engine=args.gemm_engine,
+                     pivoting=args.pivoting)
+    stage = {k: 0.0 for k in ("fill_ms", "factor_ms", "refine_ms", "solve_ms", "fields_ms")}
+
+    def step():
+        sim.compute_matrix(f0)
+        sim.set_nrhs(nrhs)
+        for c, pw in enumerate(pws):
+            sim.update_rhs(f0, pw, c)
+        sim.solve(download=False)
+        st = sim.stats()
+        sig = sim.rcs_points_multi(R_FAR, T, Pg)
+        st2 = sim.stats()
+        return sig, st, st2
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sig, st, st2 = step()
+        for k in ("fill_ms", "factor_ms", "refine_ms", "solve_ms"):
+            stage[k] += st[k]
+        stage["fields_ms"] += st2["fields_ms"]
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    clk = clocks.stop()
+    n = sim.n
+    line = {"metric": METRIC, "value": args.steps / sec, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sec / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64+c128" if args.precision == "mixed" else "c128",
+            "data": f"synthetic (seeded icosphere L{level})",
+            "config": {"workload": f"sphere_L{level}_N{n}_{f0 / 1e6:.0f}MHz_64planewaves_bistatic181x361",
+                       "n": n, "ntri": sim.nt, "precision": args.precision, "rhs": nrhs,
+                       "far_field_points": int(T.shape[0]), "z_bytes": 16 * n * n},
+            "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+            "refine_iters": st["refine_iters"], "precision_used": st["precision_used"],
+            "sigma_checksum": float(np.sum(sig)),
+            "e2e": {"value": args.steps / sec, "unit": "solves/s", "h2d_bytes_per_step": int(16 * T.shape[0]),
+                    "d2h_bytes_per_step": int(sig.nbytes)},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+    sim.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "sphere64":
+        run_sphere64(args)
     elif args.workload == "sweep":
         run_sweep(args)
     else:

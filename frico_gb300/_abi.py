@@ -20,6 +20,7 @@ HPHASE_COMPAT, HPHASE_PHYSICAL = 0, 1
 GAIN_XY, GAIN_YZ, GAIN_XZ = 0, 1, 2
 GEMM_AUTO, GEMM_SIMT, GEMM_TC = 0, 1, 2
 PIVOT_AUTO, PIVOT_PARTIAL, PIVOT_NONE = 0, 1, 2
+REFINE_AUTO, REFINE_CLASSIC = 0, 1
 
 # numpy mirror of frico_rwg (112 bytes)
 RWG_DTYPE = np.dtype([
@@ -38,7 +39,7 @@ class Options(C.Structure):
     _fields_ = [("degree", C.c_int32), ("approx", C.c_int32), ("force_symmetry", C.c_int32),
                 ("precision", C.c_int32), ("h_phase_mode", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("refine_tol", C.c_double), ("Z0", C.c_double), ("profile_kernels", C.c_int32),
-                ("gemm_engine", C.c_int32), ("pivoting", C.c_int32), ("reserved", C.c_int32)]
+                ("gemm_engine", C.c_int32), ("pivoting", C.c_int32), ("refine_mode", C.c_int32)]
 
 
 class PortValues(C.Structure):
@@ -57,7 +58,7 @@ class SweepReport(C.Structure):
                 ("lump_ms", C.c_double), ("fields_ms", C.c_double), ("lanes", C.c_int32),
                 ("autotuned", C.c_int32), ("nrhs", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("max_refine_residual", C.c_double), ("partial_pivot_fallbacks", C.c_int32),
-                ("not_converged", C.c_int32), ("fp64_fallbacks", C.c_int32), ("reserved", C.c_int32),
+                ("not_converged", C.c_int32), ("fp64_fallbacks", C.c_int32), ("fp64_direct", C.c_int32),
                 ("kernel_launches", C.c_int64)]
 
 

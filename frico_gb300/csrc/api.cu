@@ -35,6 +35,7 @@ int ensure(frico_gpu_ctx* ctx, DevBuf& b, size_t bytes) {
     if (b.bytes >= bytes) return FRICO_GPU_OK;
     if (b.p) {
         cudaStreamSynchronize(ctx->stream);
+        if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
         cudaFree(b.p);
         b.p = nullptr;
         b.bytes = 0;
@@ -76,6 +77,8 @@ static int check_options(frico_gpu_ctx* ctx, const frico_gpu_options* o) {
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown gemm_engine");
     if (o->pivoting < FRICO_PIVOT_AUTO || o->pivoting > FRICO_PIVOT_NONE)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown pivoting");
+    if (o->refine_mode != FRICO_REFINE_AUTO && o->refine_mode != FRICO_REFINE_CLASSIC)
+        return set_err(ctx, FRICO_GPU_EINVAL, "unknown refine_mode");
     return FRICO_GPU_OK;
 }
 
@@ -143,11 +146,15 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->rhs,     &ctx->sol,      &ctx->rwork,    &ctx->rwork32,   &ctx->dwork32, &ctx->norms,
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
                       &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws,   &ctx->lut,       &ctx->dinv_t,
-                      &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld};
+                      &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld,     &ctx->gm_ws};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+    for (cudaEvent_t e : ctx->la_ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return FRICO_GPU_OK;
@@ -389,7 +396,10 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
             StageTimer tm(ctx, &ctx->stats.refine_ms);
             rc = refine_solve(ctx);
         }
-        if (rc == FRICO_GPU_ENOCONV && piv == FRICO_PIVOT_AUTO && ctx->stats.pivoting_used == FRICO_PIVOT_NONE) {
+        // with classical refinement only, partial pivoting is the next thing to try; GMRES
+        // refinement already covers what pivoting would gain, so AUTO goes to FP64 directly
+        if (rc == FRICO_GPU_ENOCONV && piv == FRICO_PIVOT_AUTO && ctx->stats.pivoting_used == FRICO_PIVOT_NONE &&
+            ctx->opt.refine_mode == FRICO_REFINE_CLASSIC) {
             int rc2 = z64_to_z32(ctx);
             if (!rc2) rc2 = factor_mixed(true);
             if (rc2) return rc2;

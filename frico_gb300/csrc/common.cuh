@@ -96,6 +96,8 @@ struct DevBuf {
 struct frico_gpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // look-ahead stream of the complex64 LU
+    cudaEvent_t la_ev[2] = {nullptr, nullptr};
     frico_gpu_options opt{};
     std::string last_error;
 
@@ -138,6 +140,7 @@ struct frico_gpu_ctx {
     // adjoint: transposed factors, their inverted diagonal blocks, workspaces
     frico::DevBuf lut, dinv_t, adj_ws, adj_tab;
     frico::DevBuf mlump, mfld;    // multi-column lumped currents and field partial sums
+    frico::DevBuf gm_ws;          // GMRES refinement: Arnoldi basis and work vectors
     int32_t lumped_col = -1;
 
     frico_gpu_stats stats{};
@@ -193,9 +196,12 @@ int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw);  // 
 int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw);   // trsv.cu
 int trsv_check(frico_gpu_ctx* ctx);                           // trsv.cu
 bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
+// C (-)= L U on the tensor cores; max_ctas > 0 caps the persistent grid (leaving
+// SMs to other streams); reuse_a = 1 keeps the operand split of L from the
+// previous call with the same L, m, k.
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                    const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev,
-                   int accumulate = 1);                       // gemm_tc.cu
+                   int accumulate = 1, int max_ctas = 0, int reuse_a = 0);   // gemm_tc.cu
 int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                        const float2* U, int64_t ldu, int m, int n, int k);  // lu.cu
 int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce);  // lu.cu

@@ -373,21 +373,26 @@ bool gemm_tc_available(frico_gpu_ctx* ctx) {
 // complex64 column-major, leading dims ldc, ldl, ldu. C may alias L or U: both
 // operands are copied (split) before the MMA kernel writes C.
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl, const float2* U,
-                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev, int accumulate) {
+                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev, int accumulate, int max_ctas, int reuse_a) {
     if (m <= 0 || n <= 0 || k <= 0) return FRICO_GPU_OK;
     const int KP = ((2 * k + tc::BK - 1) / tc::BK) * tc::BK;
     const int M = 2 * m;
     const size_t a_elems = size_t(M) * KP, b_elems = size_t(n) * KP;
     int rc;
+    const size_t before = ctx->tc_ws.bytes;
     if ((rc = ensure(ctx, ctx->tc_ws, sizeof(float) * 2 * (a_elems + b_elems) + 4096))) return rc;
+    if (ctx->tc_ws.bytes != before) reuse_a = 0;   // regrown workspace (even at the same address): split again
     float* Ah = (float*)(((uintptr_t)ctx->tc_ws.p + 1023) & ~uintptr_t(1023));
     float* Al = Ah + a_elems;
     float* Bh = Al + a_elems;
     float* Bl = Bh + b_elems;
     cudaStream_t st = ctx->stream;
-    tc::k_split_a<<<(m + 31) / 32, 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al);
+    if (!reuse_a) {
+        tc::k_split_a<<<(m + 31) / 32, 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al);
+        count_launch(ctx);
+    }
     tc::k_split_b<<<unsigned((b_elems + 255) / 256), 256, 0, st>>>(U, ldu, k, n, KP, Bh, Bl);
-    count_launch(ctx, 2);
+    count_launch(ctx);
     CUtensorMap mah, mal, mbh, mbl;
     if (!make_map(&mah, Ah, M, KP) || !make_map(&mal, Al, M, KP) || !make_map(&mbh, Bh, n, KP) ||
         !make_map(&mbl, Bl, n, KP))
@@ -409,7 +414,8 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     ga.accumulate = accumulate;
     ga.st = (DeviceStatus*)ctx->status.p;
     if (ev) cudaEventRecord(ev[0], st);
-    tc::k_gemm_tf32x3<<<std::min(ntiles, sms), 192, tc::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);
+    const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
+    tc::k_gemm_tf32x3<<<std::min(ntiles, cap), 192, tc::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);
     if (ev) cudaEventRecord(ev[1], st);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");

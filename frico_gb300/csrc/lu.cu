@@ -898,8 +898,60 @@ int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb) {
     return FRICO_GPU_OK;
 }
 
+__global__ void k_matvec_reduce(int64_t cnt, int nchunks, const double2* __restrict__ part,
+                                double2* __restrict__ Y) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= cnt) return;
+    double2 acc = make_double2(0, 0);
+    for (int y = 0; y < nchunks; y++) acc = cadd(acc, part[int64_t(y) * cnt + i]);
+    Y[i] = acc;
+}
+
+// Y (n x nrhs, ld n) = Z64 X (X: n x nrhs, ld n), with the residual kernel's
+// row x column-chunk split. Workspace: ctx->rwork32.
+int matvec_fp64(frico_gpu_ctx* ctx, const double2* X, int nrhs, double2* Y) {
+    const int64_t n = ctx->n;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const unsigned rblocks = unsigned((n + 255) / 256);
+    int nchunks = std::max(1, std::min(int(n / 128), int((4 * sms + rblocks - 1) / rblocks)));
+    const int chunk = int((n + nchunks - 1) / nchunks);
+    nchunks = int((n + chunk - 1) / chunk);
+    int rc;
+    if ((rc = ensure(ctx, ctx->rwork32, sizeof(double2) * size_t(nchunks) * nrhs * n))) return rc;
+    double2* part = (double2*)ctx->rwork32.p;
+    k_residual_part<<<dim3(rblocks, nchunks), 256, 0, ctx->stream>>>((const double2*)ctx->z64.p, n, int(n), X, n,
+                                                                     nrhs, chunk, part);
+    const int64_t cnt = n * nrhs;
+    k_matvec_reduce<<<unsigned((cnt + 255) / 256), 256, 0, ctx->stream>>>(cnt, nchunks, part, Y);
+    count_launch(ctx, 2);
+    return cuda_check(ctx, cudaGetLastError(), "matvec");
+}
+
+// Out (n x nrhs, ld n) = M^{-1} In for the complex64 factors (z32, perm): rows
+// gathered by the pivot order and cast, the two chained triangular solves,
+// cast back. In has leading dimension ld_in. Workspace: ctx->dwork32.
+int precond_apply_fp32(frico_gpu_ctx* ctx, const double2* In, int64_t ld_in, int nrhs, double2* Out) {
+    const int64_t n = ctx->n, cnt = n * nrhs;
+    int rc;
+    if ((rc = ensure(ctx, ctx->dwork32, sizeof(float2) * cnt))) return rc;
+    float2* W = (float2*)ctx->dwork32.p;
+    k_gather_rows<double2, float2><<<unsigned((cnt + 255) / 256), 256, 0, ctx->stream>>>(
+        int(n), nrhs, (const int32_t*)ctx->perm.p, In, ld_in, W, n);
+    count_launch(ctx);
+    if ((rc = trsv_solve_fp32(ctx, W, nrhs, n))) return rc;
+    k_add_c64_to_c128<<<unsigned((cnt + 255) / 256), 256, 0, ctx->stream>>>(cnt, W, Out, 1);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "precond");
+}
+
+int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, const double* bnorm, double tol,
+                 int max_iters, int* iters_out, double* rel_out);   // gmres.cu
+
 // Mixed precision: X solves Z64 X = B with complex64 LU factors (z32) and FP64
-// residuals r = B - Z64 X (classical iterative refinement).
+// residuals r = B - Z64 X (classical iterative refinement). When the sweeps
+// contract too slowly (ill-conditioned Z: kappa * eps32 near 1), the same
+// factors precondition a GMRES on the FP64 system instead (gmres.cu).
 int refine_solve(frico_gpu_ctx* ctx) {
     int rc;
     const int64_t n = ctx->n;
@@ -961,7 +1013,19 @@ int refine_solve(frico_gpu_ctx* ctx) {
         if (!std::isfinite(rel)) { it++; break; }
         if (rel <= tol) { it++; break; }
         if (it >= 2 && rel > 0.5 * prev) { it++; break; }  // stagnation
+        // slow contraction: more than 6 further sweeps at this rate -> Krylov
+        if (it >= 1 && rel < prev && std::log(tol / rel) / std::log(rel / prev) > 6.0) { it++; break; }
         prev = rel;
+    }
+    if (std::isfinite(rel) && rel > tol && ctx->opt.refine_mode != FRICO_REFINE_CLASSIC) {
+        // GMRES with its own budget of 2 x max_refine_iters iterations
+        std::vector<double> bn(nrhs);
+        for (int c = 0; c < nrhs; c++) bn[c] = hn[nrhs + c] > 0 ? std::sqrt(hn[nrhs + c]) : 1.0;
+        int git = 0;
+        double grel = rel;
+        if ((rc = gmres_refine(ctx, X, B, Rr, bn.data(), tol, 2 * max_it, &git, &grel))) return rc;
+        it += git;
+        rel = grel;
     }
     ctx->stats.refine_iters = it;
     ctx->stats.refine_residual = rel;

@@ -292,6 +292,17 @@ template <typename C> __global__ void k_ipiv_identity(int n, int32_t* ipiv, int3
 
 int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce);  // lu.cu
 
+// Second stream (high priority) and two events of the look-ahead, made once per context.
+static int lookahead_streams(frico_gpu_ctx* ctx) {
+    if (ctx->stream2) return FRICO_GPU_OK;
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    int rc = cuda_check(ctx, cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, hi), "stream2");
+    for (int i = 0; !rc && i < 2; i++)
+        rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->la_ev[i], cudaEventDisableTiming), "look-ahead event");
+    return rc;
+}
+
 int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     using C = float2;
     C* A = (C*)ctx->z32.p;
@@ -323,41 +334,91 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
         return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
     k_ipiv_identity<C><<<(n + 255) / 256, 256, 0, st>>>(n, (int32_t*)ctx->ipiv.p, (int32_t*)ctx->perm.p);
     count_launch(ctx);
-    for (int k0 = 0; k0 < n; k0 += kNP) {
-        const int jb = std::min(kNP, n - k0);
-        k_diag_lu<C><<<1, 256, diag_smem, st>>>(A, lda, k0, jb, Uinv, Linv, dst);
+    if (tc) {
+        if ((rc = lookahead_streams(ctx))) return rc;
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        cudaStream_t s2 = ctx->stream2;
+        cudaEvent_t ev_narrow = ctx->la_ev[0], ev_diag = ctx->la_ev[1];
+        k_diag_lu<C><<<1, 256, diag_smem, st>>>(A, lda, 0, std::min(kNP, n), Uinv, Linv, dst);
         count_launch(ctx);
-        const int rest = n - k0 - jb;
-        if (rest > 0) {
+        bool diag_on_s2 = false;
+        for (int k0 = 0; k0 < n; k0 += kNP) {
+            const int jb = std::min(kNP, n - k0);
+            const int rest = n - k0 - jb;
+            if (diag_on_s2 && (rc = cuda_check(ctx, cudaStreamWaitEvent(st, ev_diag, 0), "wait diag"))) return rc;
+            if (rest == 0) break;
             C* A21 = A + int64_t(k0) * lda + k0 + jb;
             C* A12 = A + int64_t(k0 + jb) * lda + k0;
-            if (tc) {
-                // L21 = A21 U11^{-1},  U12 = L11^{-1} A12 on the tensor cores (overwrite mode)
-                if ((rc = gemm_update_tc(ctx, A21, lda, A21, lda, Uinv, jb, rest, jb, jb, nullptr, 0))) return rc;
-                if ((rc = gemm_update_tc(ctx, A12, lda, Linv, jb, A12, lda, jb, rest, jb, nullptr, 0))) return rc;
-            } else {
-                k_trsm_right<C><<<(rest + 63) / 64, 256, sizeof(C) * (jb * jb + 64 * jb), st>>>(A, lda, k0 + jb, n,
-                                                                                                k0, jb, Uinv);
-                count_launch(ctx);
-                if ((rc = trsm_lower_unit_f32(ctx, A, lda, k0, jb, k0 + jb, n))) return rc;
-            }
+            // L21 = A21 U11^{-1},  U12 = L11^{-1} A12 on the tensor cores (overwrite mode)
+            if ((rc = gemm_update_tc(ctx, A21, lda, A21, lda, Uinv, jb, rest, jb, jb, nullptr, 0))) return rc;
+            if ((rc = gemm_update_tc(ctx, A12, lda, Linv, jb, A12, lda, jb, rest, jb, nullptr, 0))) return rc;
+            // trailing update, next block column first; that block's LU then runs on the
+            // second stream while the rest of the update (on all but two SMs) proceeds
+            const int jb1 = std::min(kNP, rest);
             C* Cm = A + int64_t(k0 + jb) * lda + k0 + jb;
-            const C* Lm = A + int64_t(k0) * lda + k0 + jb;
-            const C* Um = A + int64_t(k0 + jb) * lda + k0;
             cudaEvent_t* ev = prof_event_pair(ctx);
             if (ev) {
-                ctx->stats.gemm_flops += 8.0 * double(rest) * double(rest) * double(jb);
-                ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(rest) + 2.0 * double(rest) * jb);
+                ctx->stats.gemm_flops += 8.0 * double(rest) * double(jb1) * double(jb);
+                ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(jb1) + double(rest) * jb + double(jb) * jb1);
             }
-            if (tc) {
-                if ((rc = gemm_update_tc(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb, ev))) return rc;
-            } else {
-                if (ev) cudaEventRecord(ev[0], st);
-                if ((rc = gemm_update_simt32(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb))) return rc;
-                if (ev) cudaEventRecord(ev[1], st);
+            if ((rc = gemm_update_tc(ctx, Cm, lda, A21, lda, A12, lda, rest, jb1, jb, ev))) return rc;
+            if ((rc = cuda_check(ctx, cudaEventRecord(ev_narrow, st), "record"))) return rc;
+            if ((rc = cuda_check(ctx, cudaStreamWaitEvent(s2, ev_narrow, 0), "wait narrow"))) return rc;
+            k_diag_lu<C><<<1, 256, diag_smem, s2>>>(A, lda, k0 + jb, jb1, Uinv, Linv, dst);
+            count_launch(ctx);
+            if ((rc = cuda_check(ctx, cudaEventRecord(ev_diag, s2), "record"))) return rc;
+            diag_on_s2 = true;
+            if (rest > jb1) {
+                const int nr = rest - jb1;
+                ev = prof_event_pair(ctx);
+                if (ev) {
+                    ctx->stats.gemm_flops += 8.0 * double(rest) * double(nr) * double(jb);
+                    ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(nr) + double(jb) * nr);
+                }
+                if ((rc = gemm_update_tc(ctx, Cm + int64_t(jb1) * lda, lda, A21, lda, A12 + int64_t(jb1) * lda, lda,
+                                         rest, nr, jb, ev, 1, std::max(1, sms - 2), 1)))
+                    return rc;
             }
+            if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
         }
-        if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
+    } else {
+        for (int k0 = 0; k0 < n; k0 += kNP) {
+            const int jb = std::min(kNP, n - k0);
+            k_diag_lu<C><<<1, 256, diag_smem, st>>>(A, lda, k0, jb, Uinv, Linv, dst);
+            count_launch(ctx);
+            const int rest = n - k0 - jb;
+            if (rest > 0) {
+                C* A21 = A + int64_t(k0) * lda + k0 + jb;
+                C* A12 = A + int64_t(k0 + jb) * lda + k0;
+                if (tc) {
+                    // L21 = A21 U11^{-1},  U12 = L11^{-1} A12 on the tensor cores (overwrite mode)
+                    if ((rc = gemm_update_tc(ctx, A21, lda, A21, lda, Uinv, jb, rest, jb, jb, nullptr, 0))) return rc;
+                    if ((rc = gemm_update_tc(ctx, A12, lda, Linv, jb, A12, lda, jb, rest, jb, nullptr, 0))) return rc;
+                } else {
+                    k_trsm_right<C><<<(rest + 63) / 64, 256, sizeof(C) * (jb * jb + 64 * jb), st>>>(A, lda, k0 + jb, n,
+                                                                                                    k0, jb, Uinv);
+                    count_launch(ctx);
+                    if ((rc = trsm_lower_unit_f32(ctx, A, lda, k0, jb, k0 + jb, n))) return rc;
+                }
+                C* Cm = A + int64_t(k0 + jb) * lda + k0 + jb;
+                const C* Lm = A + int64_t(k0) * lda + k0 + jb;
+                const C* Um = A + int64_t(k0 + jb) * lda + k0;
+                cudaEvent_t* ev = prof_event_pair(ctx);
+                if (ev) {
+                    ctx->stats.gemm_flops += 8.0 * double(rest) * double(rest) * double(jb);
+                    ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(rest) + 2.0 * double(rest) * jb);
+                }
+                if (tc) {
+                    if ((rc = gemm_update_tc(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb, ev))) return rc;
+                } else {
+                    if (ev) cudaEventRecord(ev[0], st);
+                    if ((rc = gemm_update_simt32(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb))) return rc;
+                    if (ev) cudaEventRecord(ev[1], st);
+                }
+            }
+            if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
+        }
     }
     prof_event_collect(ctx);
     DeviceStatus hs;

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -83,12 +84,31 @@ struct Tally {
     int err = FRICO_GPU_OK;
     std::string msg;
     std::atomic<bool> abort{false};
+    // Mixed precision: frequencies are visited from the highest down; once three of
+    // them have needed the FP64 factorisation, every frequency at or below the third
+    // (more ill-conditioned: the EFIE low-frequency regime) is solved in FP64
+    // directly. A single fallback can be an isolated resonance; a run of them is
+    // the low-frequency regime, where each mixed attempt costs more than FP64.
+    static constexpr int kFallbacksForDirect = 3;
+    double fp64_at_or_below = -1.0;
+    std::vector<double> fallback_freqs;
+    std::vector<int> order;   // visiting order -> frequency index
 };
 
 // One frequency on one lane, as a single-frequency caller would run it.
-int run_frequency(frico_gpu_ctx* lane, const SweepArgs& a, int fi, Tally& t) {
+int run_frequency(frico_gpu_ctx* lane, const SweepArgs& a, int fi, Tally& t, const frico_gpu_options& opt) {
     const double f = a.freqs[fi];
     const int64_t launches0 = lane->stats.kernel_launches;
+    bool direct64 = false;
+    if (opt.precision == FRICO_PREC_MIXED) {
+        std::lock_guard<std::mutex> lock(t.mu);
+        direct64 = f <= t.fp64_at_or_below;
+    }
+    frico_gpu_options o = opt;
+    if (direct64) o.precision = FRICO_PREC_FP64;
+    if (lane->opt.precision != o.precision) {
+        if (int r = frico_gpu_set_options(lane, &o)) return r;
+    }
     int rc = frico_gpu_fill(lane, f, nullptr, 0);
     if (!rc) rc = frico_gpu_set_nrhs(lane, a.nrhs);   // zeroes V (the delta gap accumulates into it)
     double rhs_ms = 0.0;
@@ -139,26 +159,37 @@ int run_frequency(frico_gpu_ctx* lane, const SweepArgs& a, int fi, Tally& t) {
     r.fields_ms += fields_ms;
     r.max_refine_iters = std::max(r.max_refine_iters, s.refine_iters);
     r.max_refine_residual = std::max(r.max_refine_residual, s.refine_residual);
-    if (lane->opt.precision == FRICO_PREC_MIXED) {
-        if (s.precision_used == FRICO_PREC_FP64)
+    if (direct64) {
+        r.fp64_direct++;
+    } else if (lane->opt.precision == FRICO_PREC_MIXED) {
+        if (s.precision_used == FRICO_PREC_FP64) {
             r.fp64_fallbacks++;
-        else if (lane->opt.pivoting != FRICO_PIVOT_PARTIAL && s.pivoting_used == FRICO_PIVOT_PARTIAL)
+            t.fallback_freqs.push_back(f);
+            if (int(t.fallback_freqs.size()) >= Tally::kFallbacksForDirect) {
+                std::vector<double> v = t.fallback_freqs;
+                std::nth_element(v.begin(), v.begin() + (Tally::kFallbacksForDirect - 1), v.end(),
+                                 std::greater<double>());
+                t.fp64_at_or_below = v[Tally::kFallbacksForDirect - 1];
+            }
+        } else if (lane->opt.pivoting != FRICO_PIVOT_PARTIAL && s.pivoting_used == FRICO_PIVOT_PARTIAL) {
             r.partial_pivot_fallbacks++;
+        }
     }
     if (noconv) r.not_converged++;
     r.kernel_launches += s.kernel_launches - launches0;
     return FRICO_GPU_OK;
 }
 
-// Frequencies [lo, hi) on lanes[0 .. nl), each lane taking the next one.
-void run_range(std::vector<frico_gpu_ctx*>& lanes, int nl, const SweepArgs& a, int lo, int hi, Tally& t) {
+// Visiting positions [lo, hi) on lanes[0 .. nl), each lane taking the next one.
+void run_range(std::vector<frico_gpu_ctx*>& lanes, int nl, const SweepArgs& a, int lo, int hi, Tally& t,
+               const frico_gpu_options& opt) {
     std::atomic<int> next{lo};
     auto worker = [&](frico_gpu_ctx* lane) {
         for (;;) {
             if (t.abort) return;
-            const int fi = next.fetch_add(1);
-            if (fi >= hi) return;
-            if (run_frequency(lane, a, fi, t)) return;
+            const int pos = next.fetch_add(1);
+            if (pos >= hi) return;
+            if (run_frequency(lane, a, t.order[pos], t, opt)) return;
         }
     };
     const int nthreads = std::min(nl, hi - lo);
@@ -182,6 +213,9 @@ int sweep(frico_gpu_ctx* ctx, const SweepArgs& a, int lanes, frico_sweep_report*
     using clock = std::chrono::steady_clock;
     const auto t0 = clock::now();
     Tally t;
+    t.order.resize(a.nfreq);
+    for (int i = 0; i < a.nfreq; i++) t.order[i] = i;
+    std::stable_sort(t.order.begin(), t.order.end(), [&](int x, int y) { return a.freqs[x] > a.freqs[y]; });
     int rc;
     // memory cap: Z64 + Z32 + factors' workspaces, about 26 N^2 bytes per lane
     size_t free_b = 0, total_b = 0;
@@ -199,13 +233,13 @@ int sweep(frico_gpu_ctx* ctx, const SweepArgs& a, int lanes, frico_sweep_report*
     int done = 0;
     if (tune) {
         // warm every candidate lane on its first frequency
-        run_range(ctx->lanes, lmax, a, 0, lmax, t);
+        run_range(ctx->lanes, lmax, a, 0, lmax, t, ctx->opt);
         done = lmax;
         double best_rate = 0.0;
         int best = 1;
         for (int l = 1; l <= lmax && !t.abort && done + l <= a.nfreq; l *= 2) {
             const auto s0 = clock::now();
-            run_range(ctx->lanes, l, a, done, done + l, t);
+            run_range(ctx->lanes, l, a, done, done + l, t, ctx->opt);
             const double sec = std::chrono::duration<double>(clock::now() - s0).count();
             done += l;
             const double rate = double(l) / std::max(sec, 1e-9);
@@ -219,7 +253,7 @@ int sweep(frico_gpu_ctx* ctx, const SweepArgs& a, int lanes, frico_sweep_report*
         nl = best;
         t.rep.autotuned = 1;
     }
-    if (!t.abort && done < a.nfreq) run_range(ctx->lanes, nl, a, done, a.nfreq, t);
+    if (!t.abort && done < a.nfreq) run_range(ctx->lanes, nl, a, done, a.nfreq, t, ctx->opt);
     t.rep.lanes = nl;
     t.rep.nrhs = a.nrhs;
     t.rep.wall_ms = std::chrono::duration<double, std::milli>(clock::now() - t0).count();

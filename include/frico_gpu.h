@@ -89,8 +89,11 @@ typedef struct frico_gpu_options {
     int32_t profile_kernels; /* 1: CUDA-event timing of every LU update GEMM */
     int32_t gemm_engine;     /* complex64 trailing update: FRICO_GEMM_AUTO or FRICO_GEMM_SIMT */
     int32_t pivoting;        /* FRICO_PIVOT_* (mixed precision only; FP64 always pivots) */
-    int32_t reserved;
+    int32_t refine_mode;     /* FRICO_REFINE_* (mixed precision only)        */
 } frico_gpu_options;
+
+#define FRICO_REFINE_AUTO    0  /* classical refinement, GMRES (2 x max_refine_iters) when it contracts slowly */
+#define FRICO_REFINE_CLASSIC 1  /* classical refinement only                                           */
 
 #define FRICO_PIVOT_AUTO    0  /* mixed: no interchanges, partial pivoting if that fails */
 #define FRICO_PIVOT_PARTIAL 1  /* LAPACK zgetrf partial pivoting                        */
@@ -251,6 +254,10 @@ int frico_gpu_eval_fields_noalloc(frico_gpu_ctx* ctx, int32_t col, int64_t npts,
  * lanes: number of concurrent frequencies; 0 chooses it (by timing the first
  * frequencies of a long sweep, else from N). The lane contexts are kept with
  * ctx for later sweeps and freed by frico_gpu_ctx_destroy.
+ * Mixed precision: frequencies are visited from the highest down; once three
+ * have fallen back to the FP64 LU, every frequency at or below the third is
+ * solved in FP64 directly (report->fp64_direct): lower frequencies are more
+ * ill-conditioned (EFIE low-frequency regime).
  * Returns the first hard error (with the frequency in the message); a
  * refinement that did not reach its tolerance at some frequency is counted in
  * report->not_converged and the call returns FRICO_GPU_ENOCONV after finishing
@@ -266,8 +273,8 @@ typedef struct frico_sweep_report {
     double  max_refine_residual;
     int32_t partial_pivot_fallbacks;  /* mixed path: frequencies factored with pivoting */
     int32_t not_converged;       /* frequencies whose refinement missed its tolerance */
-    int32_t fp64_fallbacks;      /* mixed path: frequencies solved by the FP64 LU   */
-    int32_t reserved;
+    int32_t fp64_fallbacks;      /* mixed path: frequencies that fell back to the FP64 LU */
+    int32_t fp64_direct;         /* mixed path: frequencies at or below a fallback, solved in FP64 */
     int64_t kernel_launches;     /* kernels launched by all lanes during the call   */
 } frico_sweep_report;
 

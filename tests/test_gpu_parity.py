@@ -272,13 +272,13 @@ def test_error_paths(gpu_lib, strip):
 
 def test_mixed_falls_back_to_fp64_lu_when_refinement_cannot(gpu_lib, strip):
     """When neither complex64 factorisation refines to the tolerance (here forced
-    by allowing a single refinement sweep), the mixed solve returns the FP64 LU
-    solution of the same Z and keeps those factors for further solves."""
+    by one classical sweep), the mixed solve returns the FP64 LU solution of the
+    same Z and keeps those factors for further solves."""
     f = 300e6
     fp = Simulation(strip, precision="fp64")
     fp.run_context(f, DeltaGap((meshes.FEED_TAG,), 1.0))
     Ir = fp.solve()
-    mx = Simulation(strip, precision="mixed", max_refine_iters=1)
+    mx = Simulation(strip, precision="mixed", max_refine_iters=1, refine="classic")
     mx.compute_matrix(f)
     mx.set_nrhs(1)
     mx.update_rhs(f, DeltaGap((meshes.FEED_TAG,), 1.0))
@@ -288,3 +288,24 @@ def test_mixed_falls_back_to_fp64_lu_when_refinement_cannot(gpu_lib, strip):
     np.testing.assert_array_equal(I, Ir)
     I2 = mx.solve()                       # the FP64 factors stay for further right-hand sides
     np.testing.assert_array_equal(I2, Ir)
+
+
+def test_mixed_ill_conditioned_refines_with_gmres(gpu_lib):
+    """The 1500-unknown bowtie at 250 MHz (electrically small, with skinny
+    triangles at the feed) leaves kappa * eps32 close to 1 for complex64
+    factors: classical refinement contracts too slowly, and the GMRES
+    refinement preconditioned by the same factors reaches the FP64 solution
+    without an FP64 factorisation."""
+    m = meshes.bowtie_preset(1500)
+    f = 250e6
+    dg = DeltaGap((meshes.FEED_TAG,), 1.0)
+    ref = Simulation(m, precision="fp64")
+    ref.run_context(f, dg)
+    Ir = ref.solve()
+    mx = Simulation(m, precision="mixed")
+    mx.run_context(f, dg)
+    I = mx.solve()
+    st = mx.stats()
+    assert st["precision_used"] == 1, st
+    assert st["refine_residual"] <= 1e-12
+    assert rel_norm(I, Ir) < 1e-8
