@@ -146,12 +146,14 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->rhs,     &ctx->sol,      &ctx->rwork,    &ctx->rwork32,   &ctx->dwork32, &ctx->norms,
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
                       &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws,   &ctx->lut,       &ctx->dinv_t,
-                      &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld,     &ctx->gm_ws};
+                      &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld,     &ctx->gm_ws,
+                      &ctx->dinv128};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+    if (ctx->lu_graph.exec) cudaGraphExecDestroy(ctx->lu_graph.exec);
     for (cudaEvent_t e : ctx->la_ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);

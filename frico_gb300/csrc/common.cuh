@@ -85,6 +85,15 @@ struct RwgDev {
 
 struct Ctx;
 
+// CUDA graph of the complex64 no-pivot factorisation (see lu_nopiv.cu).
+struct LuGraph {
+    uintptr_t key[10] = {};
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
+    double gemm_flops = 0.0, gemm_bytes = 0.0;
+    size_t prof_used = 0;
+};
+
 // Workspace that only grows; freed with the context.
 struct DevBuf {
     void* p = nullptr;
@@ -98,6 +107,7 @@ struct frico_gpu_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;   // look-ahead stream of the complex64 LU
     cudaEvent_t la_ev[2] = {nullptr, nullptr};
+    frico::LuGraph lu_graph;          // captured complex64 factorisation
     frico_gpu_options opt{};
     std::string last_error;
 
@@ -131,6 +141,8 @@ struct frico_gpu_ctx {
     frico::DevBuf rhs, sol, rwork, rwork32, dwork32, norms;
     frico::DevBuf dinv, trsv_flags;  // inverted diagonal blocks, chain flags + ticket
     frico::DevBuf tc_ws;             // split operands of the tensor-core trailing update
+    frico::DevBuf dinv128;           // no-pivot complex64 LU: 128 x 128 L^-1 then U^-1 blocks
+    bool dinv128_valid = false;      // dinv128 belongs to the current complex64 factors
     int trsv_epoch = 0;
     bool solved = false;
 
@@ -176,7 +188,7 @@ struct StageTimer {
 // the first time (device, key) is seen in this process and returns its status;
 // a failed init runs again on the next call. Safe to call from several host
 // threads (each driving its own context).
-enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceKeys };
+enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceTrsv128, kOnceKeys };
 int device_once(frico_gpu_ctx* ctx, OnceKey key, int (*init)(frico_gpu_ctx*));
 
 // Count one kernel launch on the context (reported as stats.kernel_launches).

@@ -133,10 +133,15 @@ struct BasisAsm {
     double v_m[3], v_p[3];   // p_free - centroid (moment expansion)
     double q_m, q_p;         // l / (2 sqrt(pi) A)
     double h_m, h_p;         // q * (degree-1 quadrature weight)
+    // signed, pre-multiplied forms for the symmetric mode-0 assembly: with
+    // u = s h a, hs = s h, hk = -s h / k^2 (s = -1 on T-, +1 on T+), a block is
+    // s_a s_b h h (a.a - 1/k^2) = u_ia.u_jb + hk_ia hs_jb
+    double u_m[3], u_p[3];
+    double hs_m, hs_p, hk_m, hk_p;
 };
 
 __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo,
-                            const double* __restrict__ qp, int nq, int mode,
+                            const double* __restrict__ qp, int nq, int mode, double inv_ksq,
                             BasisAsm* __restrict__ out) {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= n) return;
@@ -164,6 +169,14 @@ __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo
     b.q_p = s / ap;
     b.h_m = b.q_m * qm[3];
     b.h_p = b.q_p * qpp[3];
+    b.hs_m = -b.h_m;
+    b.hs_p = b.h_p;
+    b.hk_m = b.h_m * inv_ksq;
+    b.hk_p = -b.h_p * inv_ksq;
+    for (int d = 0; d < 3; d++) {
+        b.u_m[d] = b.hs_m * b.a_m[d];
+        b.u_p[d] = b.hs_p * b.a_p[d];
+    }
     out[i] = b;
 }
 
@@ -442,6 +455,82 @@ __global__ void k_symmetrize(int64_t n, int64_t ld, double2* Z) {
     }
 }
 
+// Z[j, i] of the degree-1 fill (mode 0) for basis i (column) and test j (row).
+__device__ __forceinline__ double2 entry_mode0(const AsmArgs& A, const BasisAsm& bi, const BasisAsm& bj,
+                                               int64_t i) {
+    double2 entry = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int blk = 0; blk < 4; blk++) {
+        const int s = blk >> 1, t = blk & 1;  // order --, -+, +-, ++
+        const int32_t ta = s ? bi.itp : bi.itm;
+        const int32_t tb = t ? bj.itp : bj.itm;
+        const int split = (tb == bi.itm) ? 0 : (tb == bi.itp) ? 1 : -1;
+        if (split >= 0) {
+            const double qq = (s ? bi.q_p : bi.q_m) * (t ? bj.q_p : bj.q_m);
+            const double2* m = A.S + (i * 4 + 2 * s + split) * 8;
+            const double2 F = moment_block(m, 1, s ? bi.v_p : bi.v_m, t ? bj.v_p : bj.v_m, A.inv_ksq);
+            entry = (s == t) ? cadd(entry, cscale(F, qq)) : csub(entry, cscale(F, qq));
+        } else {
+            const double* ui = s ? bi.u_p : bi.u_m;
+            const double* uj = t ? bj.u_p : bj.u_m;
+            const double f = fma(ui[0], uj[0], fma(ui[1], uj[1], fma(ui[2], uj[2], (s ? bi.hk_p : bi.hk_m) *
+                                                                                   (t ? bj.hs_p : bj.hs_m))));
+            const double2 g = A.G[int64_t(ta) * A.nt + tb];
+            entry.x = fma(g.x, f, entry.x);
+            entry.y = fma(g.y, f, entry.y);
+        }
+    }
+    return entry;
+}
+
+// Mode-0 assembly over the lower triangle of 32 x 32 tiles. Z[j, i] = Z[i, j]
+// whenever RWGs i and j share no triangle (no sub-triangle split on either side:
+// the Green table is symmetric and so is the block expression), so an
+// off-diagonal tile is computed once and also written transposed through shared
+// memory; the few pairs that share a triangle are computed in both orientations.
+__global__ void __launch_bounds__(256) k_assemble_sym0(AsmArgs A) {
+    const int64_t t = blockIdx.x;
+    int J = int((sqrt(8.0 * double(t) + 1.0) - 1.0) * 0.5);
+    while (int64_t(J) * (J + 1) / 2 > t) J--;
+    while (int64_t(J + 1) * (J + 2) / 2 <= t) J++;
+    const int I = int(t - int64_t(J) * (J + 1) / 2);   // I <= J
+    __shared__ double2 tr[32][33];
+    const int jl = threadIdx.x & 31, il0 = threadIdx.x >> 5;
+    const int64_t j = int64_t(J) * 32 + jl;
+    const bool jok = j < A.n;
+    BasisAsm bj;
+    if (jok) bj = A.bas[j];
+#pragma unroll 1
+    for (int kk = 0; kk < 4; kk++) {
+        const int il = il0 + 8 * kk;
+        const int64_t i = int64_t(I) * 32 + il;
+        if (jok && i < A.n) {
+            const BasisAsm bi = A.bas[i];
+            const double2 e = entry_mode0(A, bi, bj, i);
+            const int64_t o = i * A.ldz + j;
+            if (A.Z64) A.Z64[o] = e;
+            if (A.Z32) A.Z32[o] = make_float2(float(e.x), float(e.y));
+            if (I != J) {
+                const bool shared = bj.itm == bi.itm || bj.itm == bi.itp || bj.itp == bi.itm || bj.itp == bi.itp;
+                tr[il][jl] = shared ? entry_mode0(A, bj, bi, j) : e;   // Z[i, j]
+            }
+        }
+    }
+    if (I == J) return;
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++) {
+        const int r = threadIdx.x & 31, c = (threadIdx.x >> 5) + 8 * kk;
+        const int64_t i = int64_t(I) * 32 + r, jj = int64_t(J) * 32 + c;
+        if (i < A.n && jj < A.n) {
+            const double2 e = tr[r][c];
+            const int64_t o = jj * A.ldz + i;
+            if (A.Z64) A.Z64[o] = e;
+            if (A.Z32) A.Z32[o] = make_float2(float(e.x), float(e.y));
+        }
+    }
+}
+
 __global__ void k_z64_to_z32(int64_t count, const double2* __restrict__ a, float2* __restrict__ b) {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i < count) b[i] = make_float2(float(a[i].x), float(a[i].y));
@@ -519,7 +608,7 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     const double* qp = (const double*)ctx->qp.p;
     const double* qps = (const double*)ctx->qps.p;
     cudaStream_t st = ctx->stream;
-    k_basis_aux<<<unsigned((n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, nq, mode,
+    k_basis_aux<<<unsigned((n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, nq, mode, inv_ksq,
                                                            (BasisAsm*)ctx->basis_aux.p);
     dim3 gt(unsigned((nt + 127) / 128), unsigned(nt));
     double2* G = (double2*)ctx->gtab.p;
@@ -546,7 +635,8 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     a.Z64 = (double2*)ctx->z64.p;
     a.Z32 = want32 ? (float2*)ctx->z32.p : nullptr;
     dim3 ga(unsigned((n + 255) / 256), unsigned(n));
-    if (mode == 0) k_assemble<0><<<ga, 256, 0, st>>>(a);
+    const int64_t nbt = (n + 31) / 32;
+    if (mode == 0) k_assemble_sym0<<<unsigned(nbt * (nbt + 1) / 2), 256, 0, st>>>(a);
     else if (mode == 1) k_assemble<1><<<ga, 256, 0, st>>>(a);
     else k_assemble<2><<<ga, 256, 0, st>>>(a);
     count_launch(ctx, mode != 2 ? 4 : 3);

@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(256) k_split_a(const float2* __restrict__ L, i
                                                 float* __restrict__ Ah, float* __restrict__ Al) {
     __shared__ float2 t[32][65];
     const int r0 = blockIdx.x * 32;
-    for (int q0 = 0; q0 < KP / 2; q0 += 64) {
+    // blockIdx.y takes one 64-column chunk of K (more CTAs in flight for this store-bound copy)
+    for (int q0 = blockIdx.y * 64; q0 < min(KP / 2, (int(blockIdx.y) + 1) * 64); q0 += 64) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
             int rr = idx & 31, qq = idx >> 5;
@@ -388,7 +389,7 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     float* Bl = Bh + b_elems;
     cudaStream_t st = ctx->stream;
     if (!reuse_a) {
-        tc::k_split_a<<<(m + 31) / 32, 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al);
+        tc::k_split_a<<<dim3((m + 31) / 32, (KP / 2 + 63) / 64), 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al);
         count_launch(ctx);
     }
     tc::k_split_b<<<unsigned((b_elems + 255) / 256), 256, 0, st>>>(U, ldu, k, n, KP, Bh, Bl);

@@ -135,8 +135,9 @@ int run_frequency(frico_gpu_ctx* lane, const SweepArgs& a, int fi, Tally& t, con
     if (!rc && a.port_out && a.n_itf > 0)
         rc = frico_gpu_port_values(lane, 0, a.n_itf, a.itf_tags, a.V0, a.signs, a.port_out + fi);
     double fields_ms = 0.0;   // includes the current lumping of each column
-    for (int c = 0; !rc && a.E_out && a.npts > 0 && c < a.nrhs; c++) {
-        rc = frico_gpu_eval_fields(lane, c, a.npts, a.P, a.E_out + (int64_t(fi) * a.nrhs + c) * a.npts * 3, nullptr);
+    if (!rc && a.E_out && a.npts > 0) {   // all columns in one pass over (point, triangle) pairs
+        rc = frico_gpu_eval_fields_multi(lane, 0, a.nrhs, a.npts, a.P, a.E_out + int64_t(fi) * a.nrhs * a.npts * 3,
+                                         nullptr);
         fields_ms += lane->stats.fields_ms;
     }
     std::lock_guard<std::mutex> lock(t.mu);
@@ -207,7 +208,7 @@ int default_lanes(int64_t n) { return int(std::max<int64_t>(1, std::min<int64_t>
 
 }  // namespace
 
-static const int kTuneMinFreqs = 48;   // shorter sweeps take the lane count from N
+static const int kTuneMinFreqs = 160;  // shorter sweeps take the lane count from N
 
 int sweep(frico_gpu_ctx* ctx, const SweepArgs& a, int lanes, frico_sweep_report* report) {
     using clock = std::chrono::steady_clock;
@@ -224,7 +225,7 @@ int sweep(frico_gpu_ctx* ctx, const SweepArgs& a, int lanes, frico_sweep_report*
     const int mem_cap = int(std::max(1.0, std::min(64.0, 0.6 * double(free_b) / per_lane)));
     bool tune = lanes == 0 && a.nfreq >= kTuneMinFreqs;
     int nl = lanes > 0 ? lanes : default_lanes(a.n);
-    int lmax = std::min(16, mem_cap);
+    int lmax = std::min(32, mem_cap);
     if (tune) nl = lmax;
     nl = std::max(1, std::min(nl, std::min(mem_cap, a.nfreq)));
     if (lanes > 0 && mem_cap < std::min(lanes, a.nfreq))
@@ -237,12 +238,13 @@ int sweep(frico_gpu_ctx* ctx, const SweepArgs& a, int lanes, frico_sweep_report*
         done = lmax;
         double best_rate = 0.0;
         int best = 1;
-        for (int l = 1; l <= lmax && !t.abort && done + l <= a.nfreq; l *= 2) {
+        for (int l = 1; l <= lmax && !t.abort && done + 2 * l <= a.nfreq; l *= 2) {
+            // two frequencies per lane per round: one round is at least one full wave of l
             const auto s0 = clock::now();
-            run_range(ctx->lanes, l, a, done, done + l, t, ctx->opt);
+            run_range(ctx->lanes, l, a, done, done + 2 * l, t, ctx->opt);
             const double sec = std::chrono::duration<double>(clock::now() - s0).count();
-            done += l;
-            const double rate = double(l) / std::max(sec, 1e-9);
+            done += 2 * l;
+            const double rate = double(2 * l) / std::max(sec, 1e-9);
             if (rate > best_rate) {
                 best_rate = rate;
                 best = l;

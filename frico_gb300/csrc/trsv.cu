@@ -191,6 +191,121 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
     if (threadIdx.x == 0) atomicExch(flags + b, epoch);
 }
 
+// The same chain with 128-row blocks for the complex64 no-pivot factors, whose
+// 128 x 128 inverted diagonal blocks come out of the factorisation (column-major,
+// identity-padded past the last row): half the links of the 64-row chain, each
+// a little more work. 512 threads (row, group of 32 columns); the block's Dinv
+// is staged in shared memory before the first wait.
+constexpr int kB2 = 128;
+constexpr size_t kChain128Smem = sizeof(float2) * (size_t(kB2) * kB2 + (2 + 4 + 1) * size_t(kB2) * kRc);
+
+template <bool LOWER>
+__global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict__ LU, int64_t lda, int n,
+                                                      const float2* __restrict__ Dinv, float2* W, int64_t ldw,
+                                                      int nrhs, int* flags, unsigned* ticket, int epoch,
+                                                      DeviceStatus* st) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* Ds = (float2*)smraw;                                                  // [c * 128 + r]
+    float2 (*xs)[kB2][kRc] = reinterpret_cast<float2 (*)[kB2][kRc]>(Ds + kB2 * kB2);   // [2]
+    float2 (*part)[kB2][kRc] = xs + 2;                                            // [4]
+    float2 (*yb)[kRc] = reinterpret_cast<float2 (*)[kRc]>(part + 4);             // [128]
+    __shared__ int s_t, s_abort;
+    const int nb = (n + kB2 - 1) / kB2;
+    if (threadIdx.x == 0) {
+        s_t = int(atomicAdd(ticket, 1u));
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int t = s_t;
+    if (t >= nb) return;
+    const int b = LOWER ? t : nb - 1 - t;
+    const int r0 = b * kB2, bs = min(kB2, n - r0);
+    const int r = threadIdx.x & 127, q = threadIdx.x >> 7;   // row in block, column group (32 cols)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float2 z = make_float2(0.f, 0.f);
+
+    // independent of the chain: Dinv of this block, own right-hand side, first T block
+    const float2* D = Dinv + int64_t(b) * kB2 * kB2;
+    for (int idx = threadIdx.x; idx < kB2 * kB2; idx += 512) Ds[idx] = D[idx];
+    if (q == 0)
+#pragma unroll
+        for (int c = 0; c < kRc; c++) yb[r][c] = (r < bs && c < nrhs) ? W[int64_t(c) * ldw + r0 + r] : z;
+    float2 acc[kRc];
+#pragma unroll
+    for (int c = 0; c < kRc; c++) acc[c] = z;
+    const int ndep = LOWER ? b : nb - 1 - b;
+    float2 lv[32];
+    auto load_block = [&](int k) {
+        const int cb = LOWER ? k : nb - 1 - k;
+        const int c0 = cb * kB2, cs = min(kB2, n - c0);
+        const float2* col = LU + int64_t(c0 + q * 32) * lda + r0 + r;
+#pragma unroll
+        for (int cc = 0; cc < 32; cc++) lv[cc] = (r < bs && q * 32 + cc < cs) ? col[int64_t(cc) * lda] : z;
+    };
+    if (ndep > 0) load_block(0);
+
+    for (int k = 0; k < ndep; k++) {
+        const int cb = LOWER ? k : nb - 1 - k;
+        const int c0 = cb * kB2, cs = min(kB2, n - c0);
+        const int buf = k & 1;
+        if (warp == 0) {
+            if (lane == 0) {
+                volatile int* f = flags + cb;
+                volatile int* e = &st->err;
+                long long t0 = clock64();
+                while (*f != epoch) {
+                    if (*e) { s_abort = 1; break; }
+                    if (clock64() - t0 > kWaitCycles) {
+                        if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
+                        s_abort = 1;
+                        break;
+                    }
+                }
+            }
+            __syncwarp();
+            for (int idx = lane; idx < kB2 * nrhs; idx += 32) {
+                const int rr = idx & (kB2 - 1), c = idx >> 7;
+                xs[buf][rr][c] = rr < cs ? __ldcg(&W[int64_t(c) * ldw + c0 + rr]) : z;
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+#pragma unroll
+        for (int cc = 0; cc < 32; cc++) {
+#pragma unroll
+            for (int c = 0; c < kRc; c++)
+                if (c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[buf][q * 32 + cc][c]);
+        }
+        if (k + 1 < ndep) load_block(k + 1);   // next block's T values, while the flag is awaited
+    }
+#pragma unroll
+    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    __syncthreads();
+    if (q == 0)
+#pragma unroll
+        for (int c = 0; c < kRc; c++)
+            yb[r][c] = cadd(yb[r][c], cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c])));
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kRc; c++) acc[c] = z;
+#pragma unroll 8
+    for (int cc = 0; cc < 32; cc++) {
+        const float2 d = Ds[(q * 32 + cc) * kB2 + r];
+#pragma unroll
+        for (int c = 0; c < kRc; c++)
+            if (c < nrhs) acc[c] = cadd(acc[c], cmul(d, yb[q * 32 + cc][c]));
+    }
+#pragma unroll
+    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    __syncthreads();
+    if (q == 0 && r < bs)
+        for (int c = 0; c < nrhs; c++)
+            W[int64_t(c) * ldw + r0 + r] = cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c]));
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicExch(flags + b, epoch);
+}
+
 // ------------------------------------------------------------------ host side
 struct TrsvWs {
     void* dinv = nullptr;      // Linv blocks then Uinv blocks
@@ -203,6 +318,7 @@ template <typename C>
 int trsv_prepare(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_buf) {
     const int n = int(ctx->n), nb = (n + kB - 1) / kB;
     int rc;
+    ctx->dinv128_valid = false;   // set again by the no-pivot factorisation, which fills dinv128
     if ((rc = ensure(ctx, ws_buf, sizeof(C) * size_t(2) * nb * kB * kB))) return rc;
     if ((rc = ensure(ctx, flag_buf, sizeof(int) * (nb + 64)))) return rc;
     if ((rc = cuda_check(ctx, cudaMemsetAsync(flag_buf.p, 0, sizeof(int) * (nb + 64), ctx->stream), "flags")))
@@ -249,7 +365,41 @@ int trsv_prepare_fp32(frico_gpu_ctx* ctx) {
 int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw) {
     return trsv_solve<double2>(ctx, (const double2*)ctx->z64.p, ctx->dinv, ctx->trsv_flags, W, nrhs, ldw);
 }
+static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
+    const int n = int(ctx->n), nb = (n + kB2 - 1) / kB2, nb64 = (n + kB - 1) / kB;
+    int* flags = (int*)ctx->trsv_flags.p;
+    unsigned* ticket = (unsigned*)(flags + nb64 + 32);
+    DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
+    const float2* LU = (const float2*)ctx->z32.p;
+    const float2* Linv = (const float2*)ctx->dinv128.p;
+    const float2* Uinv = Linv + size_t(nb) * kB2 * kB2;
+    int rc = device_once(ctx, kOnceTrsv128, [](frico_gpu_ctx* c) {
+        int r = cuda_check(c, cudaFuncSetAttribute(k_trsv_chain128<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   int(kChain128Smem)), "chain128 smem");
+        if (r) return r;
+        return cuda_check(c, cudaFuncSetAttribute(k_trsv_chain128<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  int(kChain128Smem)), "chain128 smem");
+    });
+    if (rc) return rc;
+    for (int c0 = 0; c0 < nrhs; c0 += kRc) {
+        const int nc = std::min(kRc, nrhs - c0);
+        for (int pass = 0; pass < 2; pass++) {
+            const int epoch = ++ctx->trsv_epoch;
+            if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream), "ticket"))) return rc;
+            if (pass == 0)
+                k_trsv_chain128<true><<<nb, 512, kChain128Smem, ctx->stream>>>(LU, n, n, Linv, W + c0 * ldw, ldw, nc,
+                                                                                 flags, ticket, epoch, dst);
+            else
+                k_trsv_chain128<false><<<nb, 512, kChain128Smem, ctx->stream>>>(LU, n, n, Uinv, W + c0 * ldw, ldw, nc,
+                                                                                  flags, ticket, epoch, dst);
+            count_launch(ctx);
+        }
+    }
+    return cuda_check(ctx, cudaGetLastError(), "k_trsv_chain128");
+}
+
 int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
+    if (ctx->dinv128_valid) return trsv128_solve(ctx, W, nrhs, ldw);
     return trsv_solve<float2>(ctx, (const float2*)ctx->z32.p, ctx->dinv, ctx->trsv_flags, W, nrhs, ldw);
 }
 

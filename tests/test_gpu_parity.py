@@ -309,3 +309,25 @@ def test_mixed_ill_conditioned_refines_with_gmres(gpu_lib):
     assert st["precision_used"] == 1, st
     assert st["refine_residual"] <= 1e-12
     assert rel_norm(I, Ir) < 1e-8
+
+
+@pytest.mark.parametrize("profile", [False, True])
+def test_mixed_factorisation_graph_replay(gpu_lib, profile):
+    """The complex64 factorisation runs eagerly on the first call, is captured
+    into a CUDA graph on the second and replayed after that (profiling keeps it
+    eager): all three give the same currents."""
+    m = meshes.icosphere(3)
+    f = 450e6
+    sim = Simulation(m, precision="mixed", profile_kernels=profile)
+    out = []
+    for _ in range(3):
+        sim.compute_matrix(f)
+        sim.set_nrhs(1)
+        sim.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+        out.append(sim.solve()[:, 0])
+        st = sim.stats()
+        assert st["pivoting_used"] == 2 and st["refine_residual"] <= 1e-12
+    np.testing.assert_array_equal(out[0], out[1])
+    np.testing.assert_array_equal(out[0], out[2])
+    if profile:
+        assert st["gemm_launches"] > 0 and st["gemm_ms"] > 0

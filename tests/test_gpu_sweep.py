@@ -48,7 +48,8 @@ def test_sweep_equals_single_frequency_calls(gpu_lib, bowtie500, precision):
     for i, f in enumerate(freqs):
         I, pv, E = _single(ref, f, pts)
         np.testing.assert_array_equal(out["I"][i], I)
-        np.testing.assert_array_equal(out["E"][i], E)
+        # the sweep evaluates all columns in one multi-column field pass
+        assert np.abs(out["E"][i] - E).max() <= 1e-12 * np.abs(E).max()
         assert out["port"][i]["impedance"] == pv["impedance"]
 
 
@@ -71,7 +72,7 @@ def test_sweep_fp64_matches_oracle(gpu_lib, bowtie500):
 
 @pytest.mark.gpu
 def test_sweep_autotuned_lanes_give_the_same_results(gpu_lib, bowtie500):
-    freqs = meshes.sweep_frequencies(200e6, 800e6, 48)
+    freqs = meshes.sweep_frequencies(200e6, 800e6, 160)
     sim = Simulation(bowtie500, precision="mixed")
     tuned = sim.sweep(freqs, FEED, PLANE_WAVES)
     assert tuned["report"]["autotuned"] == 1 and tuned["report"]["lanes"] >= 1
