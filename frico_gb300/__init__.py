@@ -9,6 +9,12 @@ from ._abi import FricoError  # noqa: F401
 __all__ = ["meshes", "FricoError", "build", "solver"]
 
 
-def build(verbose: bool = False, force: bool = False):
+def _build(verbose: bool = False, force: bool = False):
     from .build import build as _b
+    # importing the submodule frico_gb300.build rebinds the package attribute
+    # `build` to that module; put the function back so the call can be repeated
+    globals()["build"] = _build
     return _b(verbose=verbose, force=force)
+
+
+build = _build

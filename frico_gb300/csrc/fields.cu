@@ -281,9 +281,10 @@ int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_h
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const int64_t pblocks = (npts + kFP - 1) / kFP;
-    // Enough (point block x triangle chunk) CTAs for ~8 per SM, chunks of >= 64 triangles.
-    int64_t nchunks = std::max<int64_t>(1, (int64_t(8) * sms + pblocks - 1) / pblocks);
-    nchunks = std::min<int64_t>(nchunks, std::max<int64_t>(1, nt / 64));
+    // Enough (point block x triangle chunk) CTAs for ~24 per SM (the pair loop is a
+    // long FP64 dependency chain: occupancy hides it), chunks of >= 16 triangles.
+    int64_t nchunks = std::max<int64_t>(1, (int64_t(24) * sms + pblocks - 1) / pblocks);
+    nchunks = std::min<int64_t>(nchunks, std::max<int64_t>(1, nt / 16));
     const int64_t tpc = (nt + nchunks - 1) / nchunks;
     nchunks = (nt + tpc - 1) / tpc;
     if ((rc = ensure(ctx, ctx->fld_part, sizeof(double2) * 6 * npts * nchunks))) return rc;

@@ -40,13 +40,20 @@ namespace frico {
 
 namespace tc {
 
-static const int BM = 128, BN = 128, BK = 32;    // tile rows, tile cols, floats per K slab (128 B)
-static const int STAGES = 3;
-static const int TILE_BYTES = BM * BK * 4;       // 16 KB (A and B tiles are both 128 x 32 floats)
-static const int STAGE_BYTES = 4 * TILE_BYTES;   // A hi, A lo, B hi, B lo
-static const int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-static const int TMEM_COLS = 256;
+static const int BM = 128, BK = 32;              // tile rows, floats per K slab (128 B)
 static const long long kWait = 4000000000LL;
+
+// Tile configuration by tile width BN. A stage holds A hi, A lo (128 x 32 floats
+// each) and B hi, B lo (BN x 32 floats each); the two TMEM accumulators take
+// 2 BN columns.
+template <int BN> struct Cfg {
+    static constexpr int A_TILE = BM * BK * 4;
+    static constexpr int B_TILE = BN * BK * 4;
+    static constexpr int STAGES = BN == 128 ? 3 : 2;
+    static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr int TMEM_COLS = 2 * BN;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -144,10 +151,13 @@ struct GemmArgs {
     DeviceStatus* st;
 };
 
+template <int BN>
 __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ CUtensorMap tmAh,
                                                         const __grid_constant__ CUtensorMap tmAl,
                                                         const __grid_constant__ CUtensorMap tmBh,
                                                         const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
+    constexpr int STAGES = Cfg<BN>::STAGES, STAGE_BYTES = Cfg<BN>::STAGE_BYTES;
+    constexpr int A_TILE = Cfg<BN>::A_TILE, B_TILE = Cfg<BN>::B_TILE, TMEM_COLS = Cfg<BN>::TMEM_COLS;
     extern __shared__ __align__(1024) unsigned char smraw[];
     // 1024-byte aligned ring (128-byte swizzle atoms repeat every 1024 B)
     unsigned char* ring = (unsigned char*)((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
@@ -196,9 +206,9 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
                     unsigned char* base = ring + s * STAGE_BYTES;
                     mbar_expect_tx(&full[s], STAGE_BYTES);
                     tma_load_2d(base, &tmAh, &full[s], ks * BK, mt * BM);
-                    tma_load_2d(base + TILE_BYTES, &tmAl, &full[s], ks * BK, mt * BM);
-                    tma_load_2d(base + 2 * TILE_BYTES, &tmBh, &full[s], ks * BK, nt_ * BN);
-                    tma_load_2d(base + 3 * TILE_BYTES, &tmBl, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base + A_TILE, &tmAl, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + 2 * A_TILE, &tmBh, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base + 2 * A_TILE + B_TILE, &tmBl, &full[s], ks * BK, nt_ * BN);
                 }
             }
         }
@@ -221,9 +231,9 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
                     for (int kk = 0; kk < BK / 8; kk++) {
                         const uint32_t off = uint32_t(kk * 32);   // 8 TF32 = 32 bytes along K
                         const uint64_t ah = smem_desc_sw128(base + off);
-                        const uint64_t al = smem_desc_sw128(base + TILE_BYTES + off);
-                        const uint64_t bh = smem_desc_sw128(base + 2 * TILE_BYTES + off);
-                        const uint64_t bl = smem_desc_sw128(base + 3 * TILE_BYTES + off);
+                        const uint64_t al = smem_desc_sw128(base + A_TILE + off);
+                        const uint64_t bh = smem_desc_sw128(base + 2 * A_TILE + off);
+                        const uint64_t bl = smem_desc_sw128(base + 2 * A_TILE + B_TILE + off);
                         const uint32_t first = (ks == 0 && kk == 0) ? 0u : 1u;
                         mma_tf32(tmem_d, ah, bh, idesc, first);
                         mma_tf32(tmem_d, ah, bl, idesc, 1u);
@@ -283,12 +293,12 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
 
 // A* hi/lo from the complex panel L (m x k, column-major, lda): rows 2r, 2r+1,
 // KP floats each (zero beyond 2k). A CTA handles 32 complex rows.
-__global__ void __launch_bounds__(256) k_split_a(const float2* __restrict__ L, int64_t lda, int m, int k, int KP,
-                                                float* __restrict__ Ah, float* __restrict__ Al) {
-    __shared__ float2 t[32][65];
-    const int r0 = blockIdx.x * 32;
-    // blockIdx.y takes one 64-column chunk of K (more CTAs in flight for this store-bound copy)
-    for (int q0 = blockIdx.y * 64; q0 < min(KP / 2, (int(blockIdx.y) + 1) * 64); q0 += 64) {
+__device__ __forceinline__ void split_a_tile(int bx, int by, const float2* __restrict__ L, int64_t lda, int m, int k,
+                                             int KP, float* __restrict__ Ah, float* __restrict__ Al,
+                                             float2 (*t)[65]) {
+    const int r0 = bx * 32;
+    // by takes one 64-column chunk of K (more CTAs in flight for this store-bound copy)
+    for (int q0 = by * 64; q0 < min(KP / 2, (by + 1) * 64); q0 += 64) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
             int rr = idx & 31, qq = idx >> 5;
@@ -314,9 +324,8 @@ __global__ void __launch_bounds__(256) k_split_a(const float2* __restrict__ L, i
 
 // B^ hi/lo from the complex block U (k x n, column-major, lda): row j = the
 // 2k floats of column j, zero-padded to KP.
-__global__ void k_split_b(const float2* __restrict__ U, int64_t lda, int k, int n, int KP, float* __restrict__ Bh,
-                          float* __restrict__ Bl) {
-    int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+__device__ __forceinline__ void split_b_elem(int64_t idx, const float2* __restrict__ U, int64_t lda, int k, int n,
+                                             int KP, float* __restrict__ Bh, float* __restrict__ Bl) {
     if (idx >= int64_t(n) * KP) return;
     int j = int(idx / KP), c = int(idx % KP);
     float x = 0.f;
@@ -327,6 +336,22 @@ __global__ void k_split_b(const float2* __restrict__ U, int64_t lda, int k, int 
     float hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
     Bh[idx] = hi;
     Bl[idx] = x - hi;
+}
+
+// Both operand splits of one update in a single launch: blocks [0, nA) split A
+// (32 rows x 64-column chunks of K, a_cols chunks per row band), the rest
+// split B (256 floats each). nA = 0 when the A split is reused.
+__global__ void __launch_bounds__(256) k_split_ab(const float2* __restrict__ L, int64_t ldl, int m, int k, int KP,
+                                                 float* __restrict__ Ah, float* __restrict__ Al, int nA, int a_cols,
+                                                 const float2* __restrict__ U, int64_t ldu, int n,
+                                                 float* __restrict__ Bh, float* __restrict__ Bl) {
+    __shared__ float2 t[32][65];
+    const int b = blockIdx.x;
+    if (b < nA) {
+        split_a_tile(b / a_cols, b % a_cols, L, ldl, m, k, KP, Ah, Al, t);
+    } else {
+        split_b_elem(int64_t(b - nA) * blockDim.x + threadIdx.x, U, ldu, k, n, KP, Bh, Bl);
+    }
 }
 
 }  // namespace tc
@@ -350,13 +375,13 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// rows x KP floats, row-major (K-major), box 128 rows x 32 floats, 128B swizzle.
-static bool make_map(CUtensorMap* m, float* base, int rows, int KP) {
+// rows x KP floats, row-major (K-major), box box_rows x 32 floats, 128B swizzle.
+static bool make_map(CUtensorMap* m, float* base, int rows, int KP, int box_rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[2] = {cuuint64_t(KP), cuuint64_t(rows)};
     cuuint64_t strides[1] = {cuuint64_t(KP) * 4};
-    cuuint32_t box[2] = {uint32_t(tc::BK), uint32_t(tc::BM)};
+    cuuint32_t box[2] = {uint32_t(tc::BK), uint32_t(box_rows)};
     cuuint32_t es[2] = {1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
@@ -388,24 +413,29 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     float* Bh = Al + a_elems;
     float* Bl = Bh + b_elems;
     cudaStream_t st = ctx->stream;
-    if (!reuse_a) {
-        tc::k_split_a<<<dim3((m + 31) / 32, (KP / 2 + 63) / 64), 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al);
+    {
+        const int a_cols = (KP / 2 + 63) / 64;
+        const int nA = reuse_a ? 0 : ((m + 31) / 32) * a_cols;
+        const int nB = int((b_elems + 255) / 256);
+        tc::k_split_ab<<<unsigned(nA + nB), 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al, nA, a_cols, U, ldu, n, Bh, Bl);
         count_launch(ctx);
     }
-    tc::k_split_b<<<unsigned((b_elems + 255) / 256), 256, 0, st>>>(U, ldu, k, n, KP, Bh, Bl);
-    count_launch(ctx);
+    // 128-column tiles: 256-column tiles (two stages, 25% fewer operand bytes from L2 per
+    // output) measured no faster on the LU's updates (N = 7680: 463 vs 464 TFLOP/s)
+    const int BNsel = 128;
     CUtensorMap mah, mal, mbh, mbl;
-    if (!make_map(&mah, Ah, M, KP) || !make_map(&mal, Al, M, KP) || !make_map(&mbh, Bh, n, KP) ||
-        !make_map(&mbl, Bl, n, KP))
+    if (!make_map(&mah, Ah, M, KP, tc::BM) || !make_map(&mal, Al, M, KP, tc::BM) ||
+        !make_map(&mbh, Bh, n, KP, BNsel) || !make_map(&mbl, Bl, n, KP, BNsel))
         return set_err(ctx, FRICO_GPU_ECUDA, "cuTensorMapEncodeTiled failed");
     if ((rc = device_once(ctx, kOnceGemmTc, [](frico_gpu_ctx* c) {
-             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       tc::SMEM_BYTES), "tc smem attribute");
+             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3<128>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       tc::Cfg<128>::SMEM_BYTES), "tc smem attribute");
          })))
         return rc;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const int ntiles = ((M + tc::BM - 1) / tc::BM) * ((n + tc::BN - 1) / tc::BN);
+    const int ntiles = ((M + tc::BM - 1) / tc::BM) * ((n + BNsel - 1) / BNsel);
     tc::GemmArgs ga;
     ga.C = (float*)C;
     ga.ldc = 2 * ldc;
@@ -416,7 +446,7 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     ga.st = (DeviceStatus*)ctx->status.p;
     if (ev) cudaEventRecord(ev[0], st);
     const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
-    tc::k_gemm_tf32x3<<<std::min(ntiles, cap), 192, tc::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);
+    tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), 192, tc::Cfg<128>::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);
     if (ev) cudaEventRecord(ev[1], st);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");

@@ -484,20 +484,11 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             if ((rc = launch_diag_lu(ctx, st, A, lda, k0, jb, Uinv_of(k0), Linv_of(k0), Blk, dst))) return rc;
             const int rest = n - k0 - jb;
             if (rest > 0) {
-                C* A21 = A + int64_t(k0) * lda + k0 + jb;
-                C* A12 = A + int64_t(k0 + jb) * lda + k0;
-                if (tc) {
-                    // L21 = A21 U11^{-1},  U12 = L11^{-1} A12 on the tensor cores (overwrite mode)
-                    if ((rc = gemm_update_tc(ctx, A21, lda, A21, lda, Uinv_of(k0), kNP, rest, jb, jb, nullptr, 0)))
-                        return rc;
-                    if ((rc = gemm_update_tc(ctx, A12, lda, Linv_of(k0), kNP, A12, lda, jb, rest, jb, nullptr, 0)))
-                        return rc;
-                } else {
-                    k_trsm_right<C><<<(rest + 63) / 64, 256, sizeof(C) * (jb * jb + 64 * jb), st>>>(
-                        A, lda, k0 + jb, n, k0, jb, Uinv_of(k0));
-                    count_launch(ctx);
-                    if ((rc = trsm_lower_unit_f32(ctx, A, lda, k0, jb, k0 + jb, n))) return rc;
-                }
+                // SIMT engine: L21 = A21 U11^{-1} with the inverse, U12 by the unit-lower TRSM
+                k_trsm_right<C><<<(rest + 63) / 64, 256, sizeof(C) * (jb * jb + 64 * jb), st>>>(
+                    A, lda, k0 + jb, n, k0, jb, Uinv_of(k0));
+                count_launch(ctx);
+                if ((rc = trsm_lower_unit_f32(ctx, A, lda, k0, jb, k0 + jb, n))) return rc;
                 C* Cm = A + int64_t(k0 + jb) * lda + k0 + jb;
                 const C* Lm = A + int64_t(k0) * lda + k0 + jb;
                 const C* Um = A + int64_t(k0 + jb) * lda + k0;
@@ -506,13 +497,9 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                     ctx->stats.gemm_flops += 8.0 * double(rest) * double(rest) * double(jb);
                     ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(rest) + 2.0 * double(rest) * jb);
                 }
-                if (tc) {
-                    if ((rc = gemm_update_tc(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb, ev))) return rc;
-                } else {
-                    if (ev) cudaEventRecord(ev[0], st);
-                    if ((rc = gemm_update_simt32(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb))) return rc;
-                    if (ev) cudaEventRecord(ev[1], st);
-                }
+                if (ev) cudaEventRecord(ev[0], st);
+                if ((rc = gemm_update_simt32(ctx, Cm, lda, Lm, lda, Um, lda, rest, rest, jb))) return rc;
+                if (ev) cudaEventRecord(ev[1], st);
             }
             if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
         }

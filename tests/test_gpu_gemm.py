@@ -30,6 +30,7 @@ def ctx(gpu_lib):
 
 
 @pytest.mark.parametrize("m,n,k", [(128, 128, 64), (300, 200, 64), (1000, 700, 64), (257, 129, 50), (64, 300, 17),
+                                   (1000, 700, 128), (777, 513, 128),
                                    (2048, 1536, 64)])
 @pytest.mark.parametrize("engine", ["simt", "tc"])
 def test_cgemm(gpu_lib, ctx, m, n, k, engine):
@@ -41,4 +42,5 @@ def test_cgemm(gpu_lib, ctx, m, n, k, engine):
     ref = C0.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
     out = run(gpu_lib, ctx, A, B, C0, _abi.GEMM_TC if engine == "tc" else _abi.GEMM_SIMT)
     err = np.abs(out - ref).max() / np.abs(ref).max()
-    assert err < 2e-6, err
+    # FP32 accumulation (both engines): rounding grows with the K terms summed
+    assert err < 2e-6 * max(1.0, k / 64) ** 0.75, err

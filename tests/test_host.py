@@ -112,6 +112,13 @@ def test_abi_exports_every_declared_symbol(gpu_lib):
         assert hasattr(lib, nm), nm
 
 
+def test_build_can_be_called_again_in_one_process(gpu_lib):
+    import frico_gb300
+    frico_gb300.build()
+    frico_gb300.build()
+    assert callable(frico_gb300.build)
+
+
 def test_ctx_create_without_gpu_fails_cleanly(gpu_lib):
     import torch
     if torch.cuda.is_available():
