@@ -23,8 +23,10 @@
 //               and issues tcgen05.mma (M = 128, N = 128, K = 8 per
 //               instruction); tcgen05.commit frees ring stages and publishes
 //               finished accumulators.
-//   warps 2..5  epilogue: tcgen05.ld of the accumulator (each warp its
-//               32-lane quadrant), C -= D with coalesced column loads/stores.
+//   warps 2..9  epilogue: two warps per 32-lane TMEM quadrant, 64 columns
+//               each. A warp loads its C values (64 coalesced 128-byte column
+//               segments) BEFORE it waits for the accumulator, so the C read
+//               overlaps the tile's MMAs; then tcgen05.ld, C -= D, stores.
 // All mbarrier waits are bounded; on timeout the CTA records
 // FRICO_DEV_ERR_TIMEOUT in the status word and leaves its loops.
 #include <cuda.h>
@@ -41,6 +43,8 @@ namespace frico {
 namespace tc {
 
 static const int BM = 128, BK = 32;              // tile rows, floats per K slab (128 B)
+static const int kEpiWarps = 8;                  // epilogue warps (2 per TMEM lane quadrant)
+static const int kThreads = 64 + 32 * kEpiWarps; // producer + MMA + epilogue warps
 static const long long kWait = 4000000000LL;
 
 // Tile configuration by tile width BN. A stage holds A hi, A lo (128 x 32 floats
@@ -152,12 +156,13 @@ struct GemmArgs {
 };
 
 template <int BN>
-__global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ CUtensorMap tmAh,
+__global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(const __grid_constant__ CUtensorMap tmAh,
                                                         const __grid_constant__ CUtensorMap tmAl,
                                                         const __grid_constant__ CUtensorMap tmBh,
                                                         const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
     constexpr int STAGES = Cfg<BN>::STAGES, STAGE_BYTES = Cfg<BN>::STAGE_BYTES;
     constexpr int A_TILE = Cfg<BN>::A_TILE, B_TILE = Cfg<BN>::B_TILE, TMEM_COLS = Cfg<BN>::TMEM_COLS;
+    static_assert(BN == 2 * 64, "the epilogue gives each of two warps per quadrant 64 columns");
     extern __shared__ __align__(1024) unsigned char smraw[];
     // 1024-byte aligned ring (128-byte swizzle atoms repeat every 1024 B)
     unsigned char* ring = (unsigned char*)((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(&tfull[a], 1);
-            mbar_init(&tempty[a], 4);
+            mbar_init(&tempty[a], kEpiWarps);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -246,38 +251,41 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tf32x3(const __grid_constant__ 
             }
         }
     } else {
-        // epilogue warps 2..5: TMEM lane quadrant = warp % 4
-        const int q = warp & 3;
+        // epilogue warps 2..9: TMEM lane quadrant q = warp % 4, columns [64 h, 64 h + 64)
+        const int q = warp & 3, h = ((warp - 2) >> 2) * 64;
         const int row = q * 32 + lane;
         int tcount = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, tcount++) {
             const int acc = tcount & 1, around = tcount >> 1;
             const int mt = t % tiles_m, nt_ = t / tiles_m;
+            const int gr = mt * BM + row;
+            const int ncol = min(64, g.N - nt_ * BN - h);   // columns of this warp's half (may be <= 0)
+            const bool rowok = gr < g.M;
+            float* cp = g.C + int64_t(nt_ * BN + h) * g.ldc + gr;
+            // C values first: these reads do not depend on the accumulator
+            float cv[64];
+            if (g.accumulate && rowok && ncol == 64) {
+#pragma unroll
+                for (int j = 0; j < 64; j++) cv[j] = cp[int64_t(j) * g.ldc];
+            } else {
+#pragma unroll
+                for (int j = 0; j < 64; j++) cv[j] = (g.accumulate && rowok && j < ncol) ? cp[int64_t(j) * g.ldc] : 0.f;
+            }
             if (!mbar_wait(&tfull[acc], around & 1, g.st)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int gr = mt * BM + row;
-            const uint32_t taddr = tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * BN);
-            // 64 C values of this thread's row are requested before their first
-            // use: 4 warps x 64 coalesced 128-byte requests in flight per SM.
-            const int ncol = min(BN, g.N - nt_ * BN);
-            const bool rowok = gr < g.M;
-#pragma unroll 1
-            for (int h = 0; h < BN; h += 64) {
-                const float* cp = g.C + int64_t(nt_ * BN + h) * g.ldc + gr;
-                float cv[64];
+            const uint32_t taddr = tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * BN + h);
+            // an opaque copy of the base: the store addresses are recomputed here
+            // instead of 64 load addresses being held across the wait
+            float* sp;
+            asm volatile("mov.b64 %0, %1;" : "=l"(sp) : "l"(cp));
 #pragma unroll
-                for (int j = 0; j < 64; j++)
-                    cv[j] = (g.accumulate && rowok && h + j < ncol) ? cp[int64_t(j) * g.ldc] : 0.f;
+            for (int c0 = 0; c0 < 64; c0 += 32) {
+                float v[32];
+                tmem_ld32(taddr + uint32_t(c0), v);
+                float* wp = sp + int64_t(c0) * g.ldc;
 #pragma unroll
-                for (int c0 = 0; c0 < 64; c0 += 32) {
-                    float v[32];
-                    tmem_ld32(taddr + uint32_t(h + c0), v);
-                    float* wp = g.C + int64_t(nt_ * BN + h + c0) * g.ldc + gr;
-#pragma unroll
-                    for (int j = 0; j < 32; j++)
-                        if (rowok && h + c0 + j < ncol)
-                            wp[int64_t(j) * g.ldc] = g.accumulate ? cv[c0 + j] - v[j] : v[j];
-                }
+                for (int j = 0; j < 32; j++)
+                    if (rowok && c0 + j < ncol) wp[int64_t(j) * g.ldc] = g.accumulate ? cv[c0 + j] - v[j] : v[j];
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -446,7 +454,8 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     ga.st = (DeviceStatus*)ctx->status.p;
     if (ev) cudaEventRecord(ev[0], st);
     const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
-    tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), 192, tc::Cfg<128>::SMEM_BYTES, st>>>(mah, mal, mbh, mbl, ga);
+    tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(mah, mal, mbh, mbl,
+                                                                                                  ga);
     if (ev) cudaEventRecord(ev[1], st);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");
