@@ -118,7 +118,9 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
                  int max_iters, int* iters_out, double* rel_out) {
     const int n = int(ctx->n), nrhs = ctx->nrhs;
     const int64_t cnt = int64_t(n) * nrhs;
-    const int m = std::max(1, std::min(60, max_iters));   // restart length
+    // restart length: near kappa * eps32 = 1 one Krylov space needs 40-90 vectors, and
+    // how many swings by tens with the last bits of the factors; a restart loses them
+    const int m = std::max(1, std::min(120, max_iters));
     const int64_t ldc = int64_t(m + 1) * n;   // column c's basis: V + c ldc, vector i at + i n
     cudaStream_t st = ctx->stream;
     int rc;

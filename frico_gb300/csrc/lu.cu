@@ -1018,12 +1018,13 @@ int refine_solve(frico_gpu_ctx* ctx) {
         prev = rel;
     }
     if (std::isfinite(rel) && rel > tol && ctx->opt.refine_mode != FRICO_REFINE_CLASSIC) {
-        // GMRES with its own budget of 2 x max_refine_iters iterations
+        // GMRES with its own budget: 2 x max_refine_iters iterations, at least one full
+        // Krylov space of 120
         std::vector<double> bn(nrhs);
         for (int c = 0; c < nrhs; c++) bn[c] = hn[nrhs + c] > 0 ? std::sqrt(hn[nrhs + c]) : 1.0;
         int git = 0;
         double grel = rel;
-        if ((rc = gmres_refine(ctx, X, B, Rr, bn.data(), tol, 2 * max_it, &git, &grel))) return rc;
+        if ((rc = gmres_refine(ctx, X, B, Rr, bn.data(), tol, std::max(120, 2 * max_it), &git, &grel))) return rc;
         it += git;
         rel = grel;
     }

@@ -10,8 +10,8 @@
 // pivot is zero / not finite (info != 0) or the refinement does not converge.
 //
 // Per block column k0 (width nb = 128):
-//   k_diag_lu      one CTA: LU of the nb x nb diagonal block in registers,
-//                  then U11^{-1} and L11^{-1} (triangular inverses) into a workspace
+//   k_diag_lu      two CTAs, one elimination sweep each: LU and L11^{-1} of the
+//                  nb x nb diagonal block, and U11^{-1} as the rows of U appear
 //   k_trsm_right   L21 = A21 U11^{-1}, 64 rows per CTA
 //   k_trsm_lower_unit (lu.cu)   U12 = L11^{-1} A12
 //   trailing update A22 -= L21 U12 (tensor cores when available)
@@ -30,64 +30,192 @@ static const int kNP = 128;   // block width of the no-pivot LU
 template <typename C> __device__ __forceinline__ bool cfinite(C a) { return isfinite(a.x) && isfinite(a.y); }
 
 // Diagonal block kernel: 256 threads as a 16 x 16 grid; thread (tx, ty) keeps
-// rows ty + 16 i and columns tx + 16 j (i, j < 8) of the 128 x 128 block in
-// registers. Every elimination step is a rank-1 update of the registers from
-// one column and one row published in shared memory (double-buffered, so one
-// barrier per step). Step c lies in phase P = c / 16; rows and columns of the
-// register tile below P are finished, so each phase is unrolled for its own P
-// and does only the live part of the tile.
+// rows ty + 16 i and columns tx + 16 j (i, j < 8) of a 128 x 128 working
+// matrix W in registers. Every elimination step is a rank-1 update of the
+// registers from one column and one row published in shared memory
+// (double-buffered, so one barrier per step). Step c lies in phase P = c / 16;
+// each phase is unrolled for its own P and updates only the live tiles.
+//
+// Both CTAs run the same 128 elimination steps (no interchanges) with the same
+// arithmetic on the not yet eliminated part (rows and columns > c), so they
+// see the same pivots and the same U; each keeps a different inverse in the
+// part of W that elimination has freed:
+//  CTA 1 (LOWER): row elimination of [W | I], the columns <= c of the identity
+//    half in place of the eliminated columns of W. With m_r = W[r][c] / W[c][c]:
+//      W[r][j] -= m_r W[c][j] (r > c, j != c),   W[r][c] = -m_r,
+//    ending with U on and above the diagonal and L^{-1} (unit diagonal
+//    implied) below it; the multipliers m are L.
+//  CTA 0: U^{-1} = X by a right-looking inversion as the rows of U appear. The
+//    rows r <= c hold T (columns > c) and X (columns <= c); T starts as the
+//    identity row when row c of U is final, then
+//      X[r][c] = T[r][c] / U[c][c] (r <= c),  T[r][j] -= X[r][c] U[c][j] (j > c),
+//    the same rank-1 form as the elimination of the rows below.
 static const int kDLD = kNP + 1;   // shared leading dimension (conflict-free tile reads)
 
-// LU (no interchanges), steps c = 16 P .. 16 P + 15. rdiag[c] = 1 / pivot.
-template <int P, typename C>
-__device__ __forceinline__ void diag_lu_phase(C (&v)[8][8], C* vb, C* rdiag, int tx, int ty, int k0,
-                                              DeviceStatus* st) {
+// Steps c = 16 P .. 16 P + 15. LOWER: the multipliers (L) go to S[c * kDLD + r], r > c.
+template <int P, bool LOWER, typename C>
+__device__ __forceinline__ void diag_sweep_phase(C (&v)[8][8], C* S, C* vb, int tx, int ty, int k0,
+                                                 DeviceStatus* st) {
     using R = decltype(v[0][0].x);
 #pragma unroll 1
     for (int cl = 0; cl < 16; cl++) {
         const int c = 16 * P + cl;
-        C* lb = vb + (c & 1) * 2 * kNP;   // column c (rows below the pivot)
-        C* ub = lb + kNP;                 // row c (pivot and right of it)
+        C* lb = vb + (c & 1) * 2 * kNP;   // column c (all rows)
+        C* ub = lb + kNP;                 // row c (all columns)
         if (tx == cl) {
 #pragma unroll
-            for (int i = P; i < 8; i++) lb[ty + 16 * i] = v[i][P];
+            for (int i = 0; i < 8; i++) lb[ty + 16 * i] = v[i][P];
         }
         if (ty == cl) {
 #pragma unroll
-            for (int j = P; j < 8; j++) ub[tx + 16 * j] = v[P][j];
+            for (int j = 0; j < 8; j++) ub[tx + 16 * j] = v[P][j];
         }
         __syncthreads();
         const C p = ub[c];
         const bool bad = (p.x == R(0) && p.y == R(0)) || !cfinite(p);
-        const R d = p.x * p.x + p.y * p.y;
-        const C inv = bad ? cmake(R(0), R(0)) : cmake(p.x / d, -p.y / d);
-        if (threadIdx.x == 0) {
-            rdiag[c] = inv;
-            if (bad) atomicCAS(&st->info, 0, k0 + c + 1);
-        }
-        C l[8], u[8];
+        const R rd = R(1) / (p.x * p.x + p.y * p.y);
+        const C inv = bad ? cmake(R(0), R(0)) : cmake(p.x * rd, -p.y * rd);
+        if (LOWER && bad && threadIdx.x == 0) atomicCAS(&st->info, 0, k0 + c + 1);
+        if (LOWER) {
+            C m[8], u[8];
 #pragma unroll
-        for (int i = P; i < 8; i++) l[i] = (i > P || ty > cl) ? cmul(lb[ty + 16 * i], inv) : cmake(R(0), R(0));
+            for (int i = P; i < 8; i++) m[i] = (i > P || ty > cl) ? cmul(lb[ty + 16 * i], inv) : cmake(R(0), R(0));
 #pragma unroll
-        for (int j = P; j < 8; j++) u[j] = (j > P || tx > cl) ? ub[tx + 16 * j] : cmake(R(0), R(0));
-#pragma unroll
-        for (int i = P; i < 8; i++)
-#pragma unroll
-            for (int j = P; j < 8; j++) v[i][j] = cfms(v[i][j], l[i], u[j]);
-        if (tx == cl) {
+            for (int j = 0; j < 8; j++) u[j] = ub[tx + 16 * j];
 #pragma unroll
             for (int i = P; i < 8; i++)
-                if (i > P || ty > cl) v[i][P] = l[i];
+#pragma unroll
+                for (int j = 0; j < 8; j++) v[i][j] = cfms(v[i][j], m[i], u[j]);
+            if (tx == cl) {
+#pragma unroll
+                for (int i = P; i < 8; i++)
+                    if (i > P || ty > cl) {
+                        v[i][P] = cmake(-m[i].x, -m[i].y);
+                        S[c * kDLD + ty + 16 * i] = m[i];
+                    }
+            }
+        } else {
+            // f = multiplier (rows > c), X[r][c] (rows < c), 1 / U[c][c] (row c)
+            C f[8], u[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) f[i] = (i == P && ty == cl) ? inv : cmul(lb[ty + 16 * i], inv);
+#pragma unroll
+            for (int j = P; j < 8; j++) u[j] = (j > P || tx > cl) ? ub[tx + 16 * j] : cmake(R(0), R(0));
+            if (ty == cl) {   // row c of U becomes the identity row of T
+#pragma unroll
+                for (int j = P; j < 8; j++)
+                    if (j > P || tx > cl) v[P][j] = cmake(R(0), R(0));
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = P; j < 8; j++) v[i][j] = cfms(v[i][j], f[i], u[j]);
+            if (tx == cl) {   // column c of X
+#pragma unroll
+                for (int i = 0; i <= P; i++)
+                    if (i < P || ty <= cl) v[i][P] = f[i];
+            }
         }
     }
 }
 
-// X = U^{-1} by backward column sweeps, steps i = 16 P + 15 .. 16 P:
+template <bool LOWER, typename C>
+__device__ __forceinline__ void diag_sweep(C (&v)[8][8], C* S, C* vb, int tx, int ty, int k0, DeviceStatus* st) {
+    diag_sweep_phase<0, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<1, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<2, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<3, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<4, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<5, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<6, LOWER>(v, S, vb, tx, ty, k0, st);
+    diag_sweep_phase<7, LOWER>(v, S, vb, tx, ty, k0, st);
+}
+
+template <typename C> constexpr size_t diag_lu_smem() { return sizeof(C) * (size_t(kNP) * kDLD + 4 * kNP); }
+
+// LU (no interchanges) of the jb x jb diagonal block at (k0, k0), written back
+// in place; U11^{-1} to Uinv and L11^{-1} (unit lower) to Linv, both 128 x 128
+// column-major (the GEMMs read their jb x jb part with leading dimension 128,
+// the chained solves the whole block). A block narrower than 128 is padded
+// with the identity. A zero or non-finite pivot sets st->info (first one).
+// CTA 1 writes the LU to A and L^{-1}, CTA 0 U^{-1}; both read the block from
+// `src`, a copy made before the launch (ld 128), so CTA 1 may overwrite A
+// whatever the other's timing.
+template <typename C>
+__global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0, int jb,
+                                                C* Uinv, C* Linv, DeviceStatus* st) {
+    using R = decltype(A[0].x);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C* S = (C*)smraw;              // S[c * kDLD + r]
+    C* vb = S + kNP * kDLD;        // 4 x kNP published rows / columns
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const bool lower = blockIdx.x == 1;
+#pragma unroll 16
+    for (int it = 0; it < kNP * kNP / 256; it++) {
+        const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        S[c * kDLD + r] = (r < jb && c < jb) ? src[c * kNP + r] : cmake(R(r == c ? 1 : 0), R(0));
+    }
+    __syncthreads();
+    C v[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[i][j] = S[(tx + 16 * j) * kDLD + ty + 16 * i];
+    if (lower) {
+        diag_sweep<true>(v, S, vb, tx, ty, k0, st);
+        // U (upper triangle and diagonal of W) next to L (multipliers, strict lower of S)
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
+        __syncthreads();
+#pragma unroll 16
+        for (int it = 0; it < kNP * kNP / 256; it++) {
+            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+            if (r < jb && c < jb) A[int64_t(k0 + c) * lda + k0 + r] = S[c * kDLD + r];
+        }
+        __syncthreads();   // S takes L^{-1} (strict lower of W)
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (ty + 16 * i > tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
+        __syncthreads();
+#pragma unroll 8
+        for (int it = 0; it < kNP * kNP / 256; it++) {   // full 128 x 128, identity past jb
+            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+            Linv[c * kNP + r] = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
+        }
+    } else {
+        diag_sweep<false>(v, S, vb, tx, ty, k0, st);
+        __syncthreads();   // S no longer read: it takes U^{-1} (upper triangle and diagonal of W)
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
+        __syncthreads();
+#pragma unroll 8
+        for (int it = 0; it < kNP * kNP / 256; it++) {
+            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+            Uinv[c * kNP + r] = r <= c ? S[c * kDLD + r] : cmake(R(0), R(0));
+        }
+    }
+}
+
+// U^{-1} of every diagonal block by back substitution, for the chained
+// triangular solves: the inverse from the elimination sweep satisfies
+// X U = I to working accuracy (what L21 = A21 U11^{-1} needs), the one below
+// U X = I (what the block solve x = U11^{-1} b needs); on ill-conditioned
+// blocks the two differ by far more than rounding. One CTA per block, after
+// the factorisation.
+// Backward column sweeps, steps i = 16 P + 15 .. 16 P:
 //   X[i,:] /= U[i][i];  X[k,:] -= U[k][i] X[i,:]  (k < i).
 // X[i][j] = 0 for j < i, so only tile columns >= P and rows <= P are live.
 template <int P, typename C>
-__device__ __forceinline__ void diag_uinv_phase(C (&x)[8][8], const C* S, C* vb, const C* rdiag, int tx, int ty,
-                                                int& step) {
+__device__ __forceinline__ void uinv_phase(C (&x)[8][8], const C* S, C* vb, const C* rdiag, int tx, int ty,
+                                           int& step) {
     using R = decltype(x[0][0].x);
 #pragma unroll 1
     for (int il = 15; il >= 0; il--) {
@@ -115,138 +243,57 @@ __device__ __forceinline__ void diag_uinv_phase(C (&x)[8][8], const C* S, C* vb,
     }
 }
 
-// Y = L^{-1} (unit lower) by forward column sweeps, steps i = 16 P .. 16 P + 15:
-//   Y[k,:] -= L[k][i] Y[i,:]  (k > i).  Live: tile rows >= P, columns <= P.
-template <int P, typename C>
-__device__ __forceinline__ void diag_linv_phase(C (&y)[8][8], const C* S, C* vb, int tx, int ty, int& step) {
-    using R = decltype(y[0][0].x);
-#pragma unroll 1
-    for (int il = 0; il < 16; il++) {
-        const int i = 16 * P + il;
-        C* b = vb + (step++ & 1) * kNP;
-        if (ty == il) {
-#pragma unroll
-            for (int j = 0; j <= P; j++) b[tx + 16 * j] = y[P][j];
-        }
-        __syncthreads();
-        C yr[8], cf[8];
-#pragma unroll
-        for (int j = 0; j <= P; j++) yr[j] = b[tx + 16 * j];
-#pragma unroll
-        for (int k = P; k < 8; k++) cf[k] = (k > P || ty > il) ? S[i * kDLD + ty + 16 * k] : cmake(R(0), R(0));
-#pragma unroll
-        for (int k = P; k < 8; k++)
-#pragma unroll
-            for (int j = 0; j <= P; j++) y[k][j] = cfms(y[k][j], cf[k], yr[j]);
-    }
-}
+template <typename C> constexpr size_t uinv_smem() { return sizeof(C) * (size_t(kNP) * kDLD + 3 * kNP); }
 
-template <typename C> constexpr size_t diag_lu_smem() { return sizeof(C) * (size_t(kNP) * kDLD + 5 * kNP); }
-
-// LU (no interchanges) of the jb x jb diagonal block at (k0, k0), written back
-// in place; U11^{-1} to Uinv and L11^{-1} (unit lower) to Linv, both 128 x 128
-// column-major (the GEMMs read their jb x jb part with leading dimension 128,
-// the chained solves the whole block). A block narrower than 128 is padded
-// with the identity. A zero or non-finite pivot sets st->info (first one).
-// Two CTAs (the U and the L inverse) read the block from `src`, a copy made
-// before the launch (ld 128), so CTA 0 may overwrite A whatever the other's timing.
+// Block b = blockIdx.x: U of the diagonal block at (128 b, 128 b) of A (identity
+// past n), its inverse to Uinv + b 128^2 (128 x 128 column-major).
 template <typename C>
-__global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0, int jb,
-                                                C* Uinv, C* Linv, DeviceStatus* st) {
+__global__ void __launch_bounds__(256) k_uinv_blocks(const C* __restrict__ A, int64_t lda, int n, C* Uinv) {
     using R = decltype(A[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
     C* S = (C*)smraw;              // S[c * kDLD + r]
-    C* vb = S + kNP * kDLD;        // 4 x kNP published rows / columns
-    C* rdiag = vb + 4 * kNP;       // reciprocal pivots
+    C* vb = S + kNP * kDLD;        // 2 x kNP published rows
+    C* rdiag = vb + 2 * kNP;
+    const int k0 = blockIdx.x * kNP, jb = min(kNP, n - k0);
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll 16
+    for (int idx = threadIdx.x; idx < kNP * kNP; idx += 256) {
+        const int r = idx & (kNP - 1), c = idx >> 7;
+        C a = cmake(R(r == c ? 1 : 0), R(0));
+        if (r < jb && c < jb) a = r <= c ? A[int64_t(k0 + c) * lda + k0 + r] : cmake(R(0), R(0));
+        S[c * kDLD + r] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNP) {
+        const C p = S[threadIdx.x * kDLD + threadIdx.x];
+        const R d = p.x * p.x + p.y * p.y;
+        rdiag[threadIdx.x] = d > R(0) ? cmake(p.x / d, -p.y / d) : cmake(R(0), R(0));
+    }
+    C x[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) x[i][j] = cmake(R(ty + 16 * i == tx + 16 * j ? 1 : 0), R(0));
+    int step = 0;
+    uinv_phase<7>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<6>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<5>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<4>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<3>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<2>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<1>(x, S, vb, rdiag, tx, ty, step);
+    uinv_phase<0>(x, S, vb, rdiag, tx, ty, step);
+    __syncthreads();   // U no longer read
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = x[i][j];
+    __syncthreads();
+    C* out = Uinv + size_t(blockIdx.x) * kNP * kNP;
+#pragma unroll 8
     for (int it = 0; it < kNP * kNP / 256; it++) {
         const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
-        S[c * kDLD + r] = (r < jb && c < jb) ? src[c * kNP + r] : cmake(R(r == c ? 1 : 0), R(0));
-    }
-    __syncthreads();
-    {
-        C v[8][8];
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++) v[i][j] = S[(tx + 16 * j) * kDLD + ty + 16 * i];
-        diag_lu_phase<0>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<1>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<2>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<3>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<4>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<5>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<6>(v, vb, rdiag, tx, ty, k0, st);
-        diag_lu_phase<7>(v, vb, rdiag, tx, ty, k0, st);
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
-    }
-    __syncthreads();
-    // Two CTAs factor the block identically; CTA 0 then writes the factors and
-    // inverts U, CTA 1 inverts L, so the two inverses run side by side.
-    const bool upper = blockIdx.x == 0;
-    if (upper) {
-#pragma unroll 16
-        for (int it = 0; it < kNP * kNP / 256; it++) {
-            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
-            if (r < jb && c < jb) A[int64_t(k0 + c) * lda + k0 + r] = S[c * kDLD + r];
-        }
-    }
-    int step = 0;
-    if (upper) {
-        C x[8][8];
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++) x[i][j] = cmake(R(ty + 16 * i == tx + 16 * j ? 1 : 0), R(0));
-        diag_uinv_phase<7>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<6>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<5>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<4>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<3>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<2>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<1>(x, S, vb, rdiag, tx, ty, step);
-        diag_uinv_phase<0>(x, S, vb, rdiag, tx, ty, step);
-        __syncthreads();   // U no longer read: its triangle of S takes U^{-1}
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++)
-                if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = x[i][j];
-    } else {
-        C y[8][8];
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++) y[i][j] = cmake(R(ty + 16 * i == tx + 16 * j ? 1 : 0), R(0));
-        diag_linv_phase<0>(y, S, vb, tx, ty, step);
-        diag_linv_phase<1>(y, S, vb, tx, ty, step);
-        diag_linv_phase<2>(y, S, vb, tx, ty, step);
-        diag_linv_phase<3>(y, S, vb, tx, ty, step);
-        diag_linv_phase<4>(y, S, vb, tx, ty, step);
-        diag_linv_phase<5>(y, S, vb, tx, ty, step);
-        diag_linv_phase<6>(y, S, vb, tx, ty, step);
-        diag_linv_phase<7>(y, S, vb, tx, ty, step);
-        __syncthreads();   // L no longer read: the strict lower triangle of S takes L^{-1}
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++)
-                if (ty + 16 * i > tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = y[i][j];
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int it = 0; it < kNP * kNP / 256; it++) {   // full 128 x 128, identity past jb
-        const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
-        const C s = S[c * kDLD + r];
-        const C z = cmake(R(0), R(0));
-        if (upper)
-            Uinv[c * kNP + r] = r <= c ? s : z;
-        else
-            Linv[c * kNP + r] = r > c ? s : (r == c ? cmake(R(1), R(0)) : z);
+        out[c * kNP + r] = r <= c ? S[c * kDLD + r] : cmake(R(0), R(0));
     }
 }
 
@@ -313,6 +360,14 @@ static int launch_diag_lu(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_
     k_diag_lu<float2><<<2, 256, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv, dst);
     count_launch(ctx, 2);
     return cuda_check(ctx, cudaGetLastError(), "k_diag_lu");
+}
+
+// U^{-1} of all diagonal blocks for the chained solves (replacing the sweep's).
+static int launch_uinv_blocks(frico_gpu_ctx* ctx, cudaStream_t st, const float2* A, int64_t lda, int n,
+                              float2* Uinv0) {
+    k_uinv_blocks<float2><<<(n + kNP - 1) / kNP, 256, uinv_smem<float2>(), st>>>(A, lda, n, Uinv0);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_uinv_blocks");
 }
 
 // The launch sequence of a factorisation depends only on N and on the buffers it
@@ -402,6 +457,9 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
              int r = cuda_check(c, cudaFuncSetAttribute(k_diag_lu<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         int(diag_lu_smem<float2>())), "diag smem");
              if (r) return r;
+             r = cuda_check(c, cudaFuncSetAttribute(k_uinv_blocks<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    int(uinv_smem<float2>())), "uinv smem");
+             if (r) return r;
              return cuda_check(c, cudaFuncSetAttribute(k_trsm_right<float2>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                        int(sizeof(float2) * (kNP * kNP + 64 * kNP))),
@@ -471,7 +529,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                 }
                 if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
             }
-            return FRICO_GPU_OK;
+            return launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0));
         };
         if ((rc = run_lu_graph(ctx, enqueue))) return rc;
     } else {
@@ -503,6 +561,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             }
             if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
         }
+        if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0)))) return rc;
     }
     prof_event_collect(ctx);
     DeviceStatus hs;

@@ -92,7 +92,7 @@ typedef struct frico_gpu_options {
     int32_t refine_mode;     /* FRICO_REFINE_* (mixed precision only)        */
 } frico_gpu_options;
 
-#define FRICO_REFINE_AUTO    0  /* classical refinement, GMRES (2 x max_refine_iters) when it contracts slowly */
+#define FRICO_REFINE_AUTO    0  /* classical refinement, GMRES (max(120, 2 x max_refine_iters) iterations) when it contracts slowly */
 #define FRICO_REFINE_CLASSIC 1  /* classical refinement only                                           */
 
 #define FRICO_PIVOT_AUTO    0  /* mixed: no interchanges, partial pivoting if that fails */
