@@ -21,6 +21,7 @@ GAIN_XY, GAIN_YZ, GAIN_XZ = 0, 1, 2
 GEMM_AUTO, GEMM_SIMT, GEMM_TC = 0, 1, 2
 PIVOT_AUTO, PIVOT_PARTIAL, PIVOT_NONE = 0, 1, 2
 REFINE_AUTO, REFINE_CLASSIC = 0, 1
+RESIDUAL_AUTO, RESIDUAL_FP64 = 0, 1
 
 # numpy mirror of frico_rwg (112 bytes)
 RWG_DTYPE = np.dtype([
@@ -39,7 +40,8 @@ class Options(C.Structure):
     _fields_ = [("degree", C.c_int32), ("approx", C.c_int32), ("force_symmetry", C.c_int32),
                 ("precision", C.c_int32), ("h_phase_mode", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("refine_tol", C.c_double), ("Z0", C.c_double), ("profile_kernels", C.c_int32),
-                ("gemm_engine", C.c_int32), ("pivoting", C.c_int32), ("refine_mode", C.c_int32)]
+                ("gemm_engine", C.c_int32), ("pivoting", C.c_int32), ("refine_mode", C.c_int32),
+                ("residual_mode", C.c_int32)]
 
 
 class PortValues(C.Structure):

@@ -79,6 +79,8 @@ static int check_options(frico_gpu_ctx* ctx, const frico_gpu_options* o) {
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown pivoting");
     if (o->refine_mode != FRICO_REFINE_AUTO && o->refine_mode != FRICO_REFINE_CLASSIC)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown refine_mode");
+    if (o->residual_mode != FRICO_RESIDUAL_AUTO && o->residual_mode != FRICO_RESIDUAL_FP64)
+        return set_err(ctx, FRICO_GPU_EINVAL, "unknown residual_mode");
     return FRICO_GPU_OK;
 }
 

@@ -57,7 +57,7 @@ struct DeviceStatus {
     int err;       // FRICO_DEV_ERR_* (first one wins)
     int info;      // LAPACK-style info of the last factorisation (0 = ok)
     int where;     // diagnostic: which barrier / index gave up
-    int pad;
+    int df_range;  // the double-float residual met an entry outside its exponent range
 };
 
 // ---------------------------------------------------------------- mesh on device
@@ -206,7 +206,7 @@ int trsv_prepare_fp64(frico_gpu_ctx* ctx);                    // trsv.cu
 int trsv_prepare_fp32(frico_gpu_ctx* ctx);                    // trsv.cu
 int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw);  // trsv.cu
 int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw);   // trsv.cu
-int trsv_check(frico_gpu_ctx* ctx);                           // trsv.cu
+int trsv_check(frico_gpu_ctx* ctx, DeviceStatus* out = nullptr);   // trsv.cu
 bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
 // C (-)= L U on the tensor cores; max_ctas > 0 caps the persistent grid (leaving
 // SMs to other streams); reuse_a = 1 keeps the operand split of L from the

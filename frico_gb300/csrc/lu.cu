@@ -531,6 +531,135 @@ __global__ void __launch_bounds__(256) k_residual_part(const double2* __restrict
     }
 }
 
+// The same partial products in double-float arithmetic on the FP32 pipe, which
+// is many times wider than the FP64 one on this part. Every FP64 value d is
+// split by integer operations into FP32 h + l: h = d with its significand
+// truncated to 24 bits, l = the remaining 29 bits rounded down to 23 (|d - h - l|
+// <= 2^-47 |d|). A product a b = (a1 + a2)(b1 + b2) is a1 b1 as an FP32 value
+// p plus its exact rounding error (one FMA) plus the cross terms a1 b2 + a2 b1
+// (a2 b2 < 2^-47 |a b| is dropped); p enters the running sum s by an exact
+// two-sum whose error goes to the compensation t with the small terms. (s, t)
+// is renormalised every 4 terms and flushed into FP64 every 32, so the
+// accumulated error stays below about 32 * 2^-47 of the sum of |Z[r, i] X[i]|
+// over a flush block (FP64 summation: 2^-53 per term).
+// An exponent outside [-100, 127] (values beyond about 1e-30 .. 3e38, or not
+// finite) sets st->df_range; the caller then recomputes with k_residual_part.
+__device__ __forceinline__ void split_df(double d, float& h, float& l, int& bad) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const unsigned hi = unsigned(u >> 32), lo = unsigned(u);
+    const unsigned sg = hi & 0x80000000u;
+    const int e = int((hi >> 20) & 0x7FFu);
+    const int E = e - 1023;
+    const bool zero = e == 0;   // zero or subnormal (below 1e-307): taken as zero
+    bad |= (!zero && (E < -100 || E > 127)) ? 1 : 0;
+    const int Ec = min(max(E, -100), 127);
+    const unsigned mtop = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned b = sg | (unsigned(Ec + 104) << 23);   // 2^(E-23), sign of d
+    const float hv = __uint_as_float(sg | (unsigned(Ec + 127) << 23) | mtop);
+    const float lv = __fsub_rn(__uint_as_float(b | ((lo & 0x1FFFFFFFu) >> 6)), __uint_as_float(b));
+    h = zero ? 0.f : hv;
+    l = zero ? 0.f : lv;
+}
+
+// (s, t) += a b, a = a1 + a2, b = b1 + b2
+__device__ __forceinline__ void df_mac(float& s, float& t, float a1, float a2, float b1, float b2) {
+    const float p = __fmul_rn(a1, b1);
+    float e = __fmaf_rn(a1, b1, -p);
+    e = __fmaf_rn(a1, b2, e);
+    e = __fmaf_rn(a2, b1, e);
+    const float sn = __fadd_rn(s, p);
+    const float v = __fsub_rn(sn, s);
+    t = __fadd_rn(t, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(sn, v)), __fsub_rn(p, v)), e));
+    s = sn;
+}
+
+__device__ __forceinline__ void df_renorm(float& s, float& t) {
+    const float sn = __fadd_rn(s, t);
+    t = __fsub_rn(t, __fsub_rn(sn, s));
+    s = sn;
+}
+
+// NC right-hand sides per pass (1, 2, 4 or 8: register use grows with NC);
+// 8 entries of Z are loaded ahead of their use.
+template <int NC>
+__global__ void __launch_bounds__(256) k_residual_part_df(const double2* __restrict__ Z, int64_t ldz, int n,
+                                                         const double2* __restrict__ X, int64_t ld, int nrhs,
+                                                         int chunk, double2* __restrict__ part, DeviceStatus* st) {
+    __shared__ float4 xs[128 * NC];   // (re hi, re lo, im hi, im lo) of X[i0 + ii, c0 + c]
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    int bad = 0;
+    for (int c0 = 0; c0 < nrhs; c0 += NC) {
+        const int nc = min(NC, nrhs - c0);
+        double2 acc[NC];
+        float sr[NC], tr[NC], si[NC], ti[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            acc[c] = make_double2(0, 0);
+            sr[c] = tr[c] = si[c] = ti[c] = 0.f;
+        }
+        for (int i0 = j0; i0 < j1; i0 += 128) {
+            const int ni = min(128, j1 - i0);
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < ni * nc; idx += blockDim.x) {
+                const int ii = idx % ni, c = idx / ni;
+                const double2 x = X[int64_t(c0 + c) * ld + i0 + ii];
+                float4 q;
+                split_df(x.x, q.x, q.y, bad);
+                split_df(x.y, q.z, q.w, bad);
+                xs[c * 128 + ii] = q;
+            }
+            __syncthreads();
+            if (r < n) {
+                const double2* zp = Z + int64_t(i0) * ldz + r;
+#pragma unroll 1
+                for (int b0 = 0; b0 < ni; b0 += 32) {
+                    const int be = min(b0 + 32, ni);
+#pragma unroll 1
+                    for (int ii = b0; ii < be; ii += 8) {
+                        double2 zz[8];
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            zz[u] = ii + u < be ? zp[int64_t(ii + u) * ldz] : make_double2(0, 0);
+#pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            if (ii + u >= be) break;
+                            float zr1, zr2, zi1, zi2;
+                            split_df(zz[u].x, zr1, zr2, bad);
+                            split_df(zz[u].y, zi1, zi2, bad);
+#pragma unroll
+                            for (int c = 0; c < NC; c++)
+                                if (NC == 1 || c < nc) {
+                                    const float4 x = xs[c * 128 + ii + u];
+                                    df_mac(sr[c], tr[c], zr1, zr2, x.x, x.y);     // Re += zr xr - zi xi
+                                    df_mac(sr[c], tr[c], -zi1, -zi2, x.z, x.w);
+                                    df_mac(si[c], ti[c], zr1, zr2, x.z, x.w);     // Im += zr xi + zi xr
+                                    df_mac(si[c], ti[c], zi1, zi2, x.x, x.y);
+                                    if (u == 3 || u == 7) {
+                                        df_renorm(sr[c], tr[c]);
+                                        df_renorm(si[c], ti[c]);
+                                    }
+                                }
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < NC; c++)
+                        if (NC == 1 || c < nc) {
+                            acc[c].x += double(sr[c]) + double(tr[c]);
+                            acc[c].y += double(si[c]) + double(ti[c]);
+                            sr[c] = tr[c] = si[c] = ti[c] = 0.f;
+                        }
+                }
+            }
+        }
+        if (r < n)
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+                if (c < nc) part[(int64_t(blockIdx.y) * nrhs + c0 + c) * n + r] = acc[c];
+    }
+    if (bad) atomicOr(&st->df_range, 1);
+}
+
 // R = B - sum over chunks of the partial products (fixed chunk order).
 __global__ void k_residual_reduce(int n, int nrhs, int nchunks, const double2* __restrict__ part,
                                   const double2* __restrict__ B, int64_t ld, double2* __restrict__ Rr) {
@@ -984,22 +1113,46 @@ int refine_solve(frico_gpu_ctx* ctx) {
     count_launch(ctx);
     const double2* src = B;
     double prev = 1e300, rel = 1e300;
+    DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
+    bool use_df = ctx->opt.residual_mode == FRICO_RESIDUAL_AUTO;
+    if (use_df && (rc = cuda_check(ctx, cudaMemsetAsync(&dst->df_range, 0, sizeof(int), st), "df flag"))) return rc;
+    // R = B - Z X and its column norms (double-float or FP64 products), then the norms to the host
+    auto residual = [&](bool df) -> int {
+        const double2* Z64 = (const double2*)ctx->z64.p;
+        const dim3 grid = dim3(rblocks, nchunks);
+        if (df && nrhs == 1)
+            k_residual_part_df<1><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+        else if (df && nrhs == 2)
+            k_residual_part_df<2><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+        else if (df && nrhs <= 4)
+            k_residual_part_df<4><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+        else if (df)
+            k_residual_part_df<kTR><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+        else
+            k_residual_part<<<dim3(rblocks, nchunks), 256, 0, st>>>((const double2*)ctx->z64.p, n, int(n), X, n,
+                                                                   nrhs, chunk, part);
+        k_residual_reduce<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(int(n), nrhs, nchunks, part, B, n, Rr);
+        k_colnorm2<double2><<<nrhs, 256, 0, st>>>(int(n), Rr, n, nrm);
+        count_launch(ctx, 3);
+        int r2 = cuda_check(ctx, cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st),
+                            "norms");
+        if (!r2) r2 = cuda_check(ctx, cudaStreamSynchronize(st), "refine sync");
+        return r2;
+    };
     int it = 0;
     for (; it < max_it; it++) {
         k_gather_rows<double2, float2><<<unsigned((cnt + 255) / 256), 256, 0, st>>>(
             int(n), nrhs, (const int32_t*)ctx->perm.p, src, n, W, n);
         if ((rc = trsv_solve_fp32(ctx, W, nrhs, n))) return rc;
         k_add_c64_to_c128<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, W, X, it == 0);
-        k_residual_part<<<dim3(rblocks, nchunks), 256, 0, st>>>((const double2*)ctx->z64.p, n, int(n), X, n, nrhs,
-                                                               chunk, part);
-        k_residual_reduce<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(int(n), nrhs, nchunks, part, B, n, Rr);
-        k_colnorm2<double2><<<nrhs, 256, 0, st>>>(int(n), Rr, n, nrm);
-        count_launch(ctx, 5);
-        if ((rc = cuda_check(ctx, cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs,
-                                                  cudaMemcpyDeviceToHost, st), "norms")))
-            return rc;
-        if ((rc = cuda_check(ctx, cudaStreamSynchronize(st), "refine sync"))) return rc;
-        if ((rc = trsv_check(ctx))) return rc;
+        count_launch(ctx, 2);
+        if ((rc = residual(use_df))) return rc;
+        DeviceStatus hs;
+        if ((rc = trsv_check(ctx, &hs))) return rc;
+        if (use_df && hs.df_range) {   // an entry outside the double-float range: FP64 from here on
+            use_df = false;
+            if ((rc = residual(false))) return rc;
+        }
         rel = 0.0;
         bool finite = true;
         for (int c = 0; c < nrhs; c++) {

@@ -414,12 +414,13 @@ int trsv_solve_with_fp32(frico_gpu_ctx* ctx, const float2* LU, DevBuf& dinv, flo
 }
 
 // Checks the device status word after a solve (host-synchronous).
-int trsv_check(frico_gpu_ctx* ctx) {
+int trsv_check(frico_gpu_ctx* ctx, DeviceStatus* out) {
     DeviceStatus hs;
     int rc = cuda_check(ctx, cudaMemcpyAsync(&hs, ctx->status.p, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream),
                         "status");
     if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     if (rc) return rc;
+    if (out) *out = hs;
     if (hs.err == FRICO_DEV_ERR_TIMEOUT) {
         char buf[96];
         snprintf(buf, sizeof buf, "triangular solve wait timed out at block %d", hs.where);

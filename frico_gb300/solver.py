@@ -107,7 +107,8 @@ class Simulation:
                  force_symmetry: bool = False, precision: str = "fp64", Z0: float = 50.0,
                  h_phase: str = "compat", edge_length: str = "xy", device: int = 0,
                  max_refine_iters: int = 30, refine_tol: float = 1e-12, profile_kernels: bool = False,
-                 gemm_engine: str = "auto", pivoting: str = "auto", refine: str = "auto"):
+                 gemm_engine: str = "auto", pivoting: str = "auto", refine: str = "auto",
+                 residual: str = "auto"):
         self.lib = _abi.load()
         self.mesh = mesh
         self.fs = make_function_space(mesh, edge_length)
@@ -118,7 +119,8 @@ class Simulation:
                                 {"auto": _abi.GEMM_AUTO, "simt": _abi.GEMM_SIMT, "tc": _abi.GEMM_TC}[gemm_engine],
                                 {"auto": _abi.PIVOT_AUTO, "partial": _abi.PIVOT_PARTIAL,
                                  "none": _abi.PIVOT_NONE}[pivoting],
-                                {"auto": _abi.REFINE_AUTO, "classic": _abi.REFINE_CLASSIC}[refine])
+                                {"auto": _abi.REFINE_AUTO, "classic": _abi.REFINE_CLASSIC}[refine],
+                                {"auto": _abi.RESIDUAL_AUTO, "fp64": _abi.RESIDUAL_FP64}[residual])
         self.ctx = C.c_void_p()
         rc = self.lib.frico_gpu_ctx_create(C.byref(self.ctx), device, C.byref(self.opt))
         _check(self.lib, rc, what="frico_gpu_ctx_create (is a CUDA device visible?)")

@@ -90,10 +90,14 @@ typedef struct frico_gpu_options {
     int32_t gemm_engine;     /* complex64 trailing update: FRICO_GEMM_AUTO or FRICO_GEMM_SIMT */
     int32_t pivoting;        /* FRICO_PIVOT_* (mixed precision only; FP64 always pivots) */
     int32_t refine_mode;     /* FRICO_REFINE_* (mixed precision only)        */
+    int32_t residual_mode;   /* FRICO_RESIDUAL_* (mixed precision refinement) */
 } frico_gpu_options;
 
 #define FRICO_REFINE_AUTO    0  /* classical refinement, GMRES (max(120, 2 x max_refine_iters) iterations) when it contracts slowly */
 #define FRICO_REFINE_CLASSIC 1  /* classical refinement only                                           */
+
+#define FRICO_RESIDUAL_AUTO 0  /* b - Z x in double-float on the FP32 pipe (FP64 Z split into FP32 pairs); FP64 if an entry is out of its range */
+#define FRICO_RESIDUAL_FP64 1  /* b - Z x on the FP64 pipe                                                          */
 
 #define FRICO_PIVOT_AUTO    0  /* mixed: no interchanges, partial pivoting if that fails */
 #define FRICO_PIVOT_PARTIAL 1  /* LAPACK zgetrf partial pivoting                        */
@@ -115,7 +119,7 @@ typedef struct frico_port_values {
 typedef struct frico_gpu_stats {
     double fill_ms, rhs_ms, factor_ms, solve_ms, refine_ms, lump_ms, fields_ms;
     int32_t refine_iters;
-    double  refine_residual;     /* final ||b - Z x|| / ||b|| (FP64)        */
+    double  refine_residual;     /* final ||b - Z x|| / ||b|| (FP64 sums; products per residual_mode) */
     int64_t n, ntri, nrhs;
     int64_t green_evals;         /* Green-function evaluations of last fill */
     int64_t kernel_launches;     /* kernels launched by this context so far */

@@ -185,6 +185,32 @@ def test_mixed_singular_falls_back_then_reports(gpu_lib):
     assert sim.stats()["pivoting_used"] == 1
 
 
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_double_float_residual_matches_fp64(gpu_lib, nrhs):
+    """The refinement residual in double-float (FP64 Z split into FP32 pairs on
+    the FP32 pipe) reaches the same solution as the FP64 residual, and the
+    residual it reports is the FP64 residual of the returned solution against
+    the same Z (recomputed here on the host)."""
+    m = meshes.icosphere(3)
+    f = 450e6
+    pws = [PlaneWave(0.0, 0.0, 1.0, 0.0), PlaneWave(0.7, 0.3, 0.0, 1.0), PlaneWave(1.9, 2.0, 1.0, 1.0)][:nrhs]
+    out = {}
+    for mode in ("auto", "fp64"):
+        sim = Simulation(m, precision="mixed", residual=mode)
+        Z = sim.compute_matrix(f, download=True)
+        sim.set_nrhs(nrhs)
+        for c, pw in enumerate(pws):
+            sim.update_rhs(f, pw, c)
+        B = sim.get_rhs()
+        I = sim.solve()
+        st = sim.stats()
+        assert st["refine_residual"] <= 1e-12, (mode, st["refine_residual"])
+        true = max(np.linalg.norm(B[:, c] - Z @ I[:, c]) / np.linalg.norm(B[:, c]) for c in range(nrhs))
+        assert true <= 1e-12 and abs(true - st["refine_residual"]) <= 1e-13, (mode, true, st["refine_residual"])
+        out[mode] = I
+    assert rel_norm(out["auto"], out["fp64"]) < 1e-11
+
+
 def test_mixed_strip_zin(gpu_lib, strip):
     f = 300e6
     o = oracle_for(strip)
