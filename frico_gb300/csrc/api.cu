@@ -149,7 +149,7 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
                       &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws,   &ctx->lut,       &ctx->dinv_t,
                       &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld,     &ctx->gm_ws,
-                      &ctx->dinv128};
+                      &ctx->dinv128, &ctx->trsv_x};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);

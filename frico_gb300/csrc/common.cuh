@@ -141,7 +141,8 @@ struct frico_gpu_ctx {
     frico::DevBuf rhs, sol, rwork, rwork32, dwork32, norms;
     frico::DevBuf dinv, trsv_flags;  // inverted diagonal blocks, chain flags + ticket
     frico::DevBuf tc_ws;             // split operands of the tensor-core trailing update
-    frico::DevBuf dinv128;           // no-pivot complex64 LU: 128 x 128 L^-1 then U^-1 blocks
+    frico::DevBuf dinv128;           // no-pivot complex64 LU: 128 x 128 blocks L^-1, U^-1, then the chain M blocks
+    frico::DevBuf trsv_x;            // intermediate of the 128-row chained solves
     bool dinv128_valid = false;      // dinv128 belongs to the current complex64 factors
     int trsv_epoch = 0;
     bool solved = false;
@@ -207,6 +208,7 @@ int trsv_prepare_fp32(frico_gpu_ctx* ctx);                    // trsv.cu
 int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw);  // trsv.cu
 int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw);   // trsv.cu
 int trsv_check(frico_gpu_ctx* ctx, DeviceStatus* out = nullptr);   // trsv.cu
+int trsv128_prepare(frico_gpu_ctx* ctx, cudaStream_t st);             // trsv.cu
 bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
 // C (-)= L U on the tensor cores; max_ctas > 0 caps the persistent grid (leaving
 // SMs to other streams); reuse_a = 1 keeps the operand split of L from the

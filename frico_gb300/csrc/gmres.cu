@@ -1,8 +1,8 @@
 // GMRES refinement for the mixed-precision solve (GMRES-IR): when classical
 // refinement with the complex64 factors contracts too slowly (kappa(Z) * eps32
 // close to 1: electrically small structures, the EFIE low-frequency regime),
-// the same factors become a right preconditioner for restarted GMRES on the
-// FP64 system Z d = r, with FP64 matrix-vector products against the resident
+// the same factors become a right preconditioner for restarted flexible GMRES
+// on the FP64 system Z d = r, with FP64 matrix-vector products against the resident
 // Z64 and FP64 Arnoldi vectors. Each iteration costs one preconditioner apply
 // (the two chained triangular solves), one FP64 product with Z and a
 // classical Gram-Schmidt pass repeated once (CGS2); all right-hand sides run
@@ -122,15 +122,17 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
     // how many swings by tens with the last bits of the factors; a restart loses them
     const int m = std::max(1, std::min(120, max_iters));
     const int64_t ldc = int64_t(m + 1) * n;   // column c's basis: V + c ldc, vector i at + i n
+    const int64_t ldz = int64_t(m) * n;       // preconditioned basis: Zb + c ldz, vector i at + i n
     cudaStream_t st = ctx->stream;
     int rc;
-    const size_t vbytes = sizeof(double2) * size_t(nrhs) * ldc;
+    const size_t vbytes = sizeof(double2) * size_t(nrhs) * (ldc + ldz);
     const size_t wbytes = sizeof(double2) * size_t(cnt);
     const size_t hbytes = sizeof(double2) * size_t(nrhs) * (m + 1);
     if ((rc = ensure(ctx, ctx->gm_ws, vbytes + 3 * wbytes + 3 * hbytes + sizeof(double) * 2 * nrhs + 1024)))
         return rc;
     double2* V = (double2*)ctx->gm_ws.p;
-    double2* U = V + size_t(nrhs) * ldc;
+    double2* Zb = V + size_t(nrhs) * ldc;
+    double2* U = Zb + size_t(nrhs) * ldz;
     double2* W = U + cnt;
     double2* D = W + cnt;
     double2* dh = D + cnt;                        // two CGS passes + y
@@ -181,6 +183,10 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
         int j = 0;
         for (; j < m && total < max_iters; j++, total++) {
             if ((rc = precond_apply_fp32(ctx, V + int64_t(j) * n, ldc, nrhs, U))) return rc;
+            if ((rc = cuda_check(ctx, cudaMemcpy2DAsync(Zb + int64_t(j) * n, sizeof(double2) * ldz, U,
+                                                        sizeof(double2) * n, sizeof(double2) * n, nrhs,
+                                                        cudaMemcpyDeviceToDevice, st), "gmres z")))
+                return rc;
             if ((rc = matvec_fp64(ctx, U, nrhs, W))) return rc;
             for (int pass = 0; pass < 2; pass++) {
                 double2* hp = dh + size_t(pass) * nrhs * (m + 1);
@@ -248,7 +254,9 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
             k_scale_cols<<<g1, 256, 0, st>>>(n, nrhs, W, n, dsc, V + int64_t(j + 1) * n, ldc);
             count_launch(ctx);
         }
-        // y = R^{-1} g per column, x += M^{-1} (V y)
+        // y = R^{-1} g per column, x += Z y with the stored z_i = M^{-1} v_i (flexible GMRES:
+        // applying the complex64 preconditioner once more to V y would add its rounding,
+        // which near kappa * eps32 = 1 stalls the residual above the target)
         std::fill(hy.begin(), hy.end(), double2{0.0, 0.0});
         int kmax = 0;
         for (int c = 0; c < nrhs; c++) {
@@ -267,11 +275,9 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
         if ((rc = cuda_check(ctx, cudaMemcpyAsync(dy, hy.data(), sizeof(double2) * hy.size(), cudaMemcpyHostToDevice, st),
                              "gmres y")))
             return rc;
-        k_combine<<<g1, 256, 0, st>>>(n, nrhs, kmax, V, ldc, dy, m + 1, D);
-        count_launch(ctx);
-        if ((rc = precond_apply_fp32(ctx, D, n, nrhs, U))) return rc;
-        k_add_to<<<g1, 256, 0, st>>>(cnt, U, X);
-        count_launch(ctx);
+        k_combine<<<g1, 256, 0, st>>>(n, nrhs, kmax, Zb, ldz, dy, m + 1, D);
+        k_add_to<<<g1, 256, 0, st>>>(cnt, D, X);
+        count_launch(ctx, 2);
         // true residual
         if ((rc = matvec_fp64(ctx, X, nrhs, W))) return rc;
         k_sub<<<g1, 256, 0, st>>>(cnt, B, W, R);

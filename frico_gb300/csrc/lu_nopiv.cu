@@ -446,7 +446,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
     const int nbk = (n + kNP - 1) / kNP;
     if ((rc = ensure(ctx, ctx->panel_ws, sizeof(C) * kNP * kNP + 256))) return rc;
-    if ((rc = ensure(ctx, ctx->dinv128, sizeof(C) * 2 * size_t(nbk) * kNP * kNP))) return rc;
+    if ((rc = ensure(ctx, ctx->dinv128, sizeof(C) * 4 * size_t(nbk) * kNP * kNP))) return rc;
     ctx->dinv128_valid = false;
     DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
     C* Blk = (C*)ctx->panel_ws.p;   // copy of the diagonal block being factored
@@ -529,7 +529,8 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                 }
                 if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
             }
-            return launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0));
+            if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0)))) return rc;
+            return trsv128_prepare(ctx, st);
         };
         if ((rc = run_lu_graph(ctx, enqueue))) return rc;
     } else {
@@ -562,6 +563,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
         }
         if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0)))) return rc;
+        if ((rc = trsv128_prepare(ctx, st))) return rc;
     }
     prof_event_collect(ctx);
     DeviceStatus hs;

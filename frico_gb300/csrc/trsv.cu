@@ -193,17 +193,88 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
 
 // The same chain with 128-row blocks for the complex64 no-pivot factors, whose
 // 128 x 128 inverted diagonal blocks come out of the factorisation (column-major,
-// identity-padded past the last row): half the links of the 64-row chain, each
-// a little more work. 512 threads (row, group of 32 columns); the block's Dinv
-// is staged in shared memory before the first wait.
+// identity-padded past the last row). Two changes shorten each link of the chain:
+//  * the last dependency is folded into a precomputed block: with
+//    M_b = Dinv_b T_{b,p} (p the block solved just before b),
+//      x_b = Dinv_b (w_b - sum_{c != p} T_bc x_c) - M_b x_p,
+//    so the first term is formed while x_p is still awaited and only one
+//    128 x 128 block product remains once it arrives;
+//  * results go to a buffer pre-filled with 0xFF bytes (a NaN pattern that
+//    arithmetic does not produce): a block waits for x_c by loading x_c itself
+//    until no half of it still holds the pattern, with no flag, fence or second
+//    round trip. Each 32-bit half is written once, so a half read is either the
+//    pattern or final.
+// 512 threads (row r, group q of 32 columns); Dinv_b in shared memory.
 constexpr int kB2 = 128;
 constexpr size_t kChain128Smem = sizeof(float2) * (size_t(kB2) * kB2 + (2 + 4 + 1) * size_t(kB2) * kRc);
+constexpr unsigned kUnset = 0xFFFFFFFFu;
+
+__device__ __forceinline__ float2 ld_relaxed_f2(const float2* p) {
+    float2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_f2(float2* p, float2 v) {
+    asm volatile("st.relaxed.gpu.global.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(v.x), "f"(v.y) : "memory");
+}
+
+// M_b for the chained solves: blockIdx.y = 0: Linv_b L_{b,b-1} (b >= 1), 1: Uinv_b U_{b,b+1}
+// (b <= nb - 2); 128 x 128 column-major into M + (y nb + b) 128^2. Operands go
+// through shared memory in 16-wide slabs; thread (tx, ty) owns rows ty + 16 i,
+// columns tx + 16 j.
+__global__ void __launch_bounds__(256) k_chain_mats(const float2* __restrict__ LU, int64_t lda, int n,
+                                                    const float2* __restrict__ Dinv, float2* __restrict__ M) {
+    __shared__ float2 As[kB2][17];       // As[r][k]
+    __shared__ float2 Bs[16][kB2 + 1];   // Bs[k][j]
+    const int nb = (n + kB2 - 1) / kB2, b = blockIdx.x, upper = blockIdx.y;
+    if (upper ? b >= nb - 1 : b == 0) return;
+    const float2* D = Dinv + (size_t(upper) * nb + b) * kB2 * kB2;
+    const int r0 = b * kB2, bs = min(kB2, n - r0);
+    const int cb = upper ? b + 1 : b - 1, c0 = cb * kB2, cs = min(kB2, n - c0);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float2 acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = make_float2(0.f, 0.f);
+    for (int k0 = 0; k0 < kB2; k0 += 16) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kB2 * 16; idx += 256) {
+            const int r = idx & (kB2 - 1), k = idx >> 7;
+            As[r][k] = D[int64_t(k0 + k) * kB2 + r];
+            const int kk = idx & 15, j = idx >> 4;   // T block row k0 + kk (of block b), column j (of block cb)
+            Bs[kk][j] = (k0 + kk < bs && j < cs) ? LU[int64_t(c0 + j) * lda + r0 + k0 + kk] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < 16; k++) {
+            float2 a[8], bv[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) a[i] = As[ty + 16 * i][k];
+#pragma unroll
+            for (int j = 0; j < 8; j++) bv[j] = Bs[k][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    acc[i][j].x = fmaf(a[i].x, bv[j].x, fmaf(-a[i].y, bv[j].y, acc[i][j].x));
+                    acc[i][j].y = fmaf(a[i].x, bv[j].y, fmaf(a[i].y, bv[j].x, acc[i][j].y));
+                }
+        }
+    }
+    float2* out = M + (size_t(upper) * nb + b) * kB2 * kB2;
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) out[(tx + 16 * j) * kB2 + ty + 16 * i] = acc[i][j];
+}
 
 template <bool LOWER>
 __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict__ LU, int64_t lda, int n,
-                                                      const float2* __restrict__ Dinv, float2* W, int64_t ldw,
-                                                      int nrhs, int* flags, unsigned* ticket, int epoch,
-                                                      DeviceStatus* st) {
+                                                      const float2* __restrict__ Dinv, const float2* __restrict__ M,
+                                                      const float2* __restrict__ Win, int64_t ldin, float2* Xout,
+                                                      int64_t ldout, int nrhs, unsigned* ticket, DeviceStatus* st) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* Ds = (float2*)smraw;                                                  // [c * 128 + r]
     float2 (*xs)[kB2][kRc] = reinterpret_cast<float2 (*)[kB2][kRc]>(Ds + kB2 * kB2);   // [2]
@@ -229,46 +300,59 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
     for (int idx = threadIdx.x; idx < kB2 * kB2; idx += 512) Ds[idx] = D[idx];
     if (q == 0)
 #pragma unroll
-        for (int c = 0; c < kRc; c++) yb[r][c] = (r < bs && c < nrhs) ? W[int64_t(c) * ldw + r0 + r] : z;
+        for (int c = 0; c < kRc; c++) yb[r][c] = (r < bs && c < nrhs) ? Win[int64_t(c) * ldin + r0 + r] : z;
     float2 acc[kRc];
 #pragma unroll
     for (int c = 0; c < kRc; c++) acc[c] = z;
     const int ndep = LOWER ? b : nb - 1 - b;
     float2 lv[32];
+    // T block of dependency k, or M_b for the last one (rows of this block, 32 columns of group q)
     auto load_block = [&](int k) {
-        const int cb = LOWER ? k : nb - 1 - k;
-        const int c0 = cb * kB2, cs = min(kB2, n - c0);
-        const float2* col = LU + int64_t(c0 + q * 32) * lda + r0 + r;
+        if (k == ndep - 1) {
+            const float2* m = M + int64_t(b) * kB2 * kB2 + int64_t(q * 32) * kB2 + r;
 #pragma unroll
-        for (int cc = 0; cc < 32; cc++) lv[cc] = (r < bs && q * 32 + cc < cs) ? col[int64_t(cc) * lda] : z;
+            for (int cc = 0; cc < 32; cc++) lv[cc] = m[cc * kB2];
+        } else {
+            const int cb = LOWER ? k : nb - 1 - k;
+            const int c0 = cb * kB2, cs = min(kB2, n - c0);
+            const float2* col = LU + int64_t(c0 + q * 32) * lda + r0 + r;
+#pragma unroll
+            for (int cc = 0; cc < 32; cc++) lv[cc] = (r < bs && q * 32 + cc < cs) ? col[int64_t(cc) * lda] : z;
+        }
     };
-    if (ndep > 0) load_block(0);
-
-    for (int k = 0; k < ndep; k++) {
-        const int cb = LOWER ? k : nb - 1 - k;
-        const int c0 = cb * kB2, cs = min(kB2, n - c0);
-        const int buf = k & 1;
+    // x of block column cb into xs[buf] once every value of it is final (warp 0; bounded wait)
+    auto await_x = [&](int cb, int buf) {
         if (warp == 0) {
-            if (lane == 0) {
-                volatile int* f = flags + cb;
-                volatile int* e = &st->err;
-                long long t0 = clock64();
-                while (*f != epoch) {
-                    if (*e) { s_abort = 1; break; }
-                    if (clock64() - t0 > kWaitCycles) {
-                        if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
-                        s_abort = 1;
-                        break;
+            const int c0 = cb * kB2, cs = min(kB2, n - c0);
+            long long t0 = clock64();
+            volatile int* e = &st->err;
+            while (true) {
+                bool pending = false;
+                for (int idx = lane; idx < kB2 * nrhs; idx += 32) {
+                    const int rr = idx & (kB2 - 1), c = idx >> 7;
+                    float2 v = z;
+                    if (rr < cs) {
+                        v = ld_relaxed_f2(&Xout[int64_t(c) * ldout + c0 + rr]);
+                        pending |= __float_as_uint(v.x) == kUnset || __float_as_uint(v.y) == kUnset;
                     }
+                    xs[buf][rr][c] = v;
                 }
-            }
-            __syncwarp();
-            for (int idx = lane; idx < kB2 * nrhs; idx += 32) {
-                const int rr = idx & (kB2 - 1), c = idx >> 7;
-                xs[buf][rr][c] = rr < cs ? __ldcg(&W[int64_t(c) * ldw + c0 + rr]) : z;
+                if (!__any_sync(0xffffffffu, pending)) break;
+                if (lane == 0 && (*e || clock64() - t0 > kWaitCycles)) {
+                    if (!*e && atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
+                    s_abort = 1;
+                }
+                if (__shfl_sync(0xffffffffu, s_abort, 0)) break;
             }
         }
         __syncthreads();
+    };
+    if (ndep > 0) load_block(0);
+
+    for (int k = 0; k < ndep - 1; k++) {
+        const int cb = LOWER ? k : nb - 1 - k;
+        const int buf = k & 1;
+        await_x(cb, buf);
         if (s_abort) return;
 #pragma unroll
         for (int cc = 0; cc < 32; cc++) {
@@ -276,8 +360,9 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
             for (int c = 0; c < kRc; c++)
                 if (c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[buf][q * 32 + cc][c]);
         }
-        if (k + 1 < ndep) load_block(k + 1);   // next block's T values, while the flag is awaited
+        load_block(k + 1);   // next block's T values (or M_b), while the next x is awaited
     }
+    // y' = Dinv_b (w_b - sum over all but the last dependency), before the last x is in
 #pragma unroll
     for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
     __syncthreads();
@@ -298,12 +383,35 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
 #pragma unroll
     for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
     __syncthreads();
-    if (q == 0 && r < bs)
-        for (int c = 0; c < nrhs; c++)
-            W[int64_t(c) * ldw + r0 + r] = cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c]));
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) atomicExch(flags + b, epoch);
+    if (q == 0)
+#pragma unroll
+        for (int c = 0; c < kRc; c++)
+            yb[r][c] = cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c]));
+    // the last dependency: x_b = y' - M_b x_p
+    if (ndep > 0) {
+        const int kl = ndep - 1, cb = LOWER ? kl : nb - 1 - kl;
+        await_x(cb, kl & 1);   // (its barrier also publishes yb)
+        if (s_abort) return;
+#pragma unroll
+        for (int c = 0; c < kRc; c++) acc[c] = z;
+#pragma unroll
+        for (int cc = 0; cc < 32; cc++) {
+#pragma unroll
+            for (int c = 0; c < kRc; c++)
+                if (c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[kl & 1][q * 32 + cc][c]);
+        }
+#pragma unroll
+        for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+        __syncthreads();
+        if (q == 0 && r < bs)
+            for (int c = 0; c < nrhs; c++)
+                st_relaxed_f2(&Xout[int64_t(c) * ldout + r0 + r],
+                              cadd(yb[r][c], cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c]))));
+    } else {
+        __syncthreads();
+        if (q == 0 && r < bs)
+            for (int c = 0; c < nrhs; c++) st_relaxed_f2(&Xout[int64_t(c) * ldout + r0 + r], yb[r][c]);
+    }
 }
 
 // ------------------------------------------------------------------ host side
@@ -365,6 +473,17 @@ int trsv_prepare_fp32(frico_gpu_ctx* ctx) {
 int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw) {
     return trsv_solve<double2>(ctx, (const double2*)ctx->z64.p, ctx->dinv, ctx->trsv_flags, W, nrhs, ldw);
 }
+// M blocks of the 128-row chains (after dinv128's L^{-1}, U^{-1} blocks), once per factorisation.
+int trsv128_prepare(frico_gpu_ctx* ctx, cudaStream_t st) {
+    const int n = int(ctx->n), nb = (n + kB2 - 1) / kB2;
+    const float2* Dinv = (const float2*)ctx->dinv128.p;
+    k_chain_mats<<<dim3(nb, 2), 256, 0, st>>>((const float2*)ctx->z32.p, n, n, Dinv,
+                                              (float2*)ctx->dinv128.p + size_t(2) * nb * kB2 * kB2);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_chain_mats");
+}
+
+// Lower pass W -> X (scratch), upper pass X -> W; each output pre-filled with the pattern.
 static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     const int n = int(ctx->n), nb = (n + kB2 - 1) / kB2, nb64 = (n + kB - 1) / kB;
     int* flags = (int*)ctx->trsv_flags.p;
@@ -373,6 +492,9 @@ static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     const float2* LU = (const float2*)ctx->z32.p;
     const float2* Linv = (const float2*)ctx->dinv128.p;
     const float2* Uinv = Linv + size_t(nb) * kB2 * kB2;
+    const float2* Mlow = Linv + size_t(2) * nb * kB2 * kB2;
+    const float2* Mup = Linv + size_t(3) * nb * kB2 * kB2;
+    cudaStream_t st = ctx->stream;
     int rc = device_once(ctx, kOnceTrsv128, [](frico_gpu_ctx* c) {
         int r = cuda_check(c, cudaFuncSetAttribute(k_trsv_chain128<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    int(kChain128Smem)), "chain128 smem");
@@ -381,19 +503,20 @@ static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
                                                   int(kChain128Smem)), "chain128 smem");
     });
     if (rc) return rc;
+    if ((rc = ensure(ctx, ctx->trsv_x, sizeof(float2) * size_t(n) * kRc))) return rc;
+    float2* X = (float2*)ctx->trsv_x.p;
     for (int c0 = 0; c0 < nrhs; c0 += kRc) {
         const int nc = std::min(kRc, nrhs - c0);
-        for (int pass = 0; pass < 2; pass++) {
-            const int epoch = ++ctx->trsv_epoch;
-            if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream), "ticket"))) return rc;
-            if (pass == 0)
-                k_trsv_chain128<true><<<nb, 512, kChain128Smem, ctx->stream>>>(LU, n, n, Linv, W + c0 * ldw, ldw, nc,
-                                                                                 flags, ticket, epoch, dst);
-            else
-                k_trsv_chain128<false><<<nb, 512, kChain128Smem, ctx->stream>>>(LU, n, n, Uinv, W + c0 * ldw, ldw, nc,
-                                                                                  flags, ticket, epoch, dst);
-            count_launch(ctx);
-        }
+        float2* Wc = W + c0 * ldw;
+        if ((rc = cuda_check(ctx, cudaMemsetAsync(X, 0xFF, sizeof(float2) * size_t(n) * nc, st), "unset x"))) return rc;
+        if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "ticket"))) return rc;
+        k_trsv_chain128<true><<<nb, 512, kChain128Smem, st>>>(LU, n, n, Linv, Mlow, Wc, ldw, X, n, nc, ticket, dst);
+        if ((rc = cuda_check(ctx, cudaMemset2DAsync(Wc, sizeof(float2) * ldw, 0xFF, sizeof(float2) * n, nc, st),
+                             "unset w")))
+            return rc;
+        if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "ticket"))) return rc;
+        k_trsv_chain128<false><<<nb, 512, kChain128Smem, st>>>(LU, n, n, Uinv, Mup, X, n, Wc, ldw, nc, ticket, dst);
+        count_launch(ctx, 2);
     }
     return cuda_check(ctx, cudaGetLastError(), "k_trsv_chain128");
 }
