@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(256) k_chain_mats(const float2* __restrict__ L
         for (int j = 0; j < 8; j++) out[(tx + 16 * j) * kB2 + ty + 16 * i] = acc[i][j];
 }
 
-template <bool LOWER>
+// NC: right-hand sides per launch (1, 2, 4 or 8), a compile-time bound on the column loops
+template <bool LOWER, int NC>
 __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict__ LU, int64_t lda, int n,
                                                       const float2* __restrict__ Dinv, const float2* __restrict__ M,
                                                       const float2* __restrict__ Win, int64_t ldin, float2* Xout,
@@ -300,10 +301,10 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
     for (int idx = threadIdx.x; idx < kB2 * kB2; idx += 512) Ds[idx] = D[idx];
     if (q == 0)
 #pragma unroll
-        for (int c = 0; c < kRc; c++) yb[r][c] = (r < bs && c < nrhs) ? Win[int64_t(c) * ldin + r0 + r] : z;
-    float2 acc[kRc];
+        for (int c = 0; c < NC; c++) yb[r][c] = (r < bs && c < nrhs) ? Win[int64_t(c) * ldin + r0 + r] : z;
+    float2 acc[NC];
 #pragma unroll
-    for (int c = 0; c < kRc; c++) acc[c] = z;
+    for (int c = 0; c < NC; c++) acc[c] = z;
     const int ndep = LOWER ? b : nb - 1 - b;
     float2 lv[32];
     // T block of dependency k, or M_b for the last one (rows of this block, 32 columns of group q)
@@ -357,35 +358,35 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
 #pragma unroll
         for (int cc = 0; cc < 32; cc++) {
 #pragma unroll
-            for (int c = 0; c < kRc; c++)
-                if (c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[buf][q * 32 + cc][c]);
+            for (int c = 0; c < NC; c++)
+                if (NC == 1 || c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[buf][q * 32 + cc][c]);
         }
         load_block(k + 1);   // next block's T values (or M_b), while the next x is awaited
     }
     // y' = Dinv_b (w_b - sum over all but the last dependency), before the last x is in
 #pragma unroll
-    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    for (int c = 0; c < NC; c++) part[q][r][c] = acc[c];
     __syncthreads();
     if (q == 0)
 #pragma unroll
-        for (int c = 0; c < kRc; c++)
+        for (int c = 0; c < NC; c++)
             yb[r][c] = cadd(yb[r][c], cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c])));
     __syncthreads();
 #pragma unroll
-    for (int c = 0; c < kRc; c++) acc[c] = z;
+    for (int c = 0; c < NC; c++) acc[c] = z;
 #pragma unroll 8
     for (int cc = 0; cc < 32; cc++) {
         const float2 d = Ds[(q * 32 + cc) * kB2 + r];
 #pragma unroll
-        for (int c = 0; c < kRc; c++)
-            if (c < nrhs) acc[c] = cadd(acc[c], cmul(d, yb[q * 32 + cc][c]));
+        for (int c = 0; c < NC; c++)
+            if (NC == 1 || c < nrhs) acc[c] = cadd(acc[c], cmul(d, yb[q * 32 + cc][c]));
     }
 #pragma unroll
-    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    for (int c = 0; c < NC; c++) part[q][r][c] = acc[c];
     __syncthreads();
     if (q == 0)
 #pragma unroll
-        for (int c = 0; c < kRc; c++)
+        for (int c = 0; c < NC; c++)
             yb[r][c] = cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c]));
     // the last dependency: x_b = y' - M_b x_p
     if (ndep > 0) {
@@ -393,15 +394,15 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
         await_x(cb, kl & 1);   // (its barrier also publishes yb)
         if (s_abort) return;
 #pragma unroll
-        for (int c = 0; c < kRc; c++) acc[c] = z;
+        for (int c = 0; c < NC; c++) acc[c] = z;
 #pragma unroll
         for (int cc = 0; cc < 32; cc++) {
 #pragma unroll
-            for (int c = 0; c < kRc; c++)
-                if (c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[kl & 1][q * 32 + cc][c]);
+            for (int c = 0; c < NC; c++)
+                if (NC == 1 || c < nrhs) acc[c] = cfms(acc[c], lv[cc], xs[kl & 1][q * 32 + cc][c]);
         }
 #pragma unroll
-        for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+        for (int c = 0; c < NC; c++) part[q][r][c] = acc[c];
         __syncthreads();
         if (q == 0 && r < bs)
             for (int c = 0; c < nrhs; c++)
@@ -483,6 +484,21 @@ int trsv128_prepare(frico_gpu_ctx* ctx, cudaStream_t st) {
     return cuda_check(ctx, cudaGetLastError(), "k_chain_mats");
 }
 
+template <bool LOWER>
+static void launch_chain128(int nc, int nb, cudaStream_t st, const float2* LU, int n, const float2* D,
+                            const float2* M, const float2* Win, int64_t ldin, float2* Xout, int64_t ldout,
+                            unsigned* ticket, DeviceStatus* dst) {
+    if (nc == 1)
+        k_trsv_chain128<LOWER, 1><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst);
+    else if (nc == 2)
+        k_trsv_chain128<LOWER, 2><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst);
+    else if (nc <= 4)
+        k_trsv_chain128<LOWER, 4><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst);
+    else
+        k_trsv_chain128<LOWER, kRc><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket,
+                                                                     dst);
+}
+
 // Lower pass W -> X (scratch), upper pass X -> W; each output pre-filled with the pattern.
 static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     const int n = int(ctx->n), nb = (n + kB2 - 1) / kB2, nb64 = (n + kB - 1) / kB;
@@ -496,11 +512,16 @@ static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     const float2* Mup = Linv + size_t(3) * nb * kB2 * kB2;
     cudaStream_t st = ctx->stream;
     int rc = device_once(ctx, kOnceTrsv128, [](frico_gpu_ctx* c) {
-        int r = cuda_check(c, cudaFuncSetAttribute(k_trsv_chain128<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   int(kChain128Smem)), "chain128 smem");
-        if (r) return r;
-        return cuda_check(c, cudaFuncSetAttribute(k_trsv_chain128<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  int(kChain128Smem)), "chain128 smem");
+        const void* fns[8] = {(const void*)k_trsv_chain128<true, 1>,   (const void*)k_trsv_chain128<true, 2>,
+                              (const void*)k_trsv_chain128<true, 4>,   (const void*)k_trsv_chain128<true, kRc>,
+                              (const void*)k_trsv_chain128<false, 1>,  (const void*)k_trsv_chain128<false, 2>,
+                              (const void*)k_trsv_chain128<false, 4>,  (const void*)k_trsv_chain128<false, kRc>};
+        for (const void* f : fns) {
+            int r = cuda_check(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kChain128Smem)),
+                               "chain128 smem");
+            if (r) return r;
+        }
+        return 0;
     });
     if (rc) return rc;
     if ((rc = ensure(ctx, ctx->trsv_x, sizeof(float2) * size_t(n) * kRc))) return rc;
@@ -510,12 +531,12 @@ static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
         float2* Wc = W + c0 * ldw;
         if ((rc = cuda_check(ctx, cudaMemsetAsync(X, 0xFF, sizeof(float2) * size_t(n) * nc, st), "unset x"))) return rc;
         if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "ticket"))) return rc;
-        k_trsv_chain128<true><<<nb, 512, kChain128Smem, st>>>(LU, n, n, Linv, Mlow, Wc, ldw, X, n, nc, ticket, dst);
+        launch_chain128<true>(nc, nb, st, LU, n, Linv, Mlow, Wc, ldw, X, n, ticket, dst);
         if ((rc = cuda_check(ctx, cudaMemset2DAsync(Wc, sizeof(float2) * ldw, 0xFF, sizeof(float2) * n, nc, st),
                              "unset w")))
             return rc;
         if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "ticket"))) return rc;
-        k_trsv_chain128<false><<<nb, 512, kChain128Smem, st>>>(LU, n, n, Uinv, Mup, X, n, Wc, ldw, nc, ticket, dst);
+        launch_chain128<false>(nc, nb, st, LU, n, Uinv, Mup, X, n, Wc, ldw, ticket, dst);
         count_launch(ctx, 2);
     }
     return cuda_check(ctx, cudaGetLastError(), "k_trsv_chain128");
