@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(128) k_invert_diag(const C* __restrict__ LU, i
 // Critical path per chain link: flag seen by warp 0 -> warp 0 loads the
 // published block (double-buffered, one barrier) -> 16 FMAs per thread from
 // prefetched registers -> reduction -> Dinv (prefetched) -> store, fence, flag.
-template <typename C, bool LOWER>
+template <typename C, bool LOWER, int NC>
 __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, int64_t lda, int n, const C* __restrict__ Dinv,
                                                    C* W, int64_t ldw, int nrhs, int* flags, unsigned* ticket, int epoch,
                                                    DeviceStatus* st) {
@@ -102,15 +102,15 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
     // independent of the chain: own right-hand side (into yb), Dinv block, first T block
     if (q == 0)
 #pragma unroll
-        for (int c = 0; c < kRc; c++)
+        for (int c = 0; c < NC; c++)
             yb[r][c] = (r < bs && c < nrhs) ? W[int64_t(c) * ldw + r0 + r] : cmake(R(0), R(0));
     const C* D = Dinv + int64_t(b) * kB * kB;
     C dv[16];
 #pragma unroll
     for (int cc = 0; cc < 16; cc++) dv[cc] = (r < bs && q * 16 + cc < bs) ? D[(q * 16 + cc) * kB + r] : cmake(R(0), R(0));
-    C acc[kRc];
+    C acc[NC];
 #pragma unroll
-    for (int c = 0; c < kRc; c++) acc[c] = cmake(R(0), R(0));
+    for (int c = 0; c < NC; c++) acc[c] = cmake(R(0), R(0));
     const int ndep = LOWER ? b : nb - 1 - b;
     C lv[16];
     auto load_block = [&](int k) {
@@ -158,30 +158,30 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
 #pragma unroll
         for (int cc = 0; cc < 16; cc++) {
 #pragma unroll
-            for (int c = 0; c < kRc; c++)
-                if (c < nrhs) acc[c] = cfms(acc[c], cur[cc], xs[buf][q * 16 + cc][c]);
+            for (int c = 0; c < NC; c++)
+                if (NC == 1 || c < nrhs) acc[c] = cfms(acc[c], cur[cc], xs[buf][q * 16 + cc][c]);
         }
     }
     // y_pre = w_b + sum of the four partial sums
 #pragma unroll
-    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    for (int c = 0; c < NC; c++) part[q][r][c] = acc[c];
     __syncthreads();
     if (q == 0)
 #pragma unroll
-        for (int c = 0; c < kRc; c++)
+        for (int c = 0; c < NC; c++)
             yb[r][c] = cadd(yb[r][c], cadd(cadd(part[0][r][c], part[1][r][c]), cadd(part[2][r][c], part[3][r][c])));
     __syncthreads();
     // y = Dinv_b * y_pre
 #pragma unroll
-    for (int c = 0; c < kRc; c++) acc[c] = cmake(R(0), R(0));
+    for (int c = 0; c < NC; c++) acc[c] = cmake(R(0), R(0));
 #pragma unroll
     for (int cc = 0; cc < 16; cc++) {
 #pragma unroll
-        for (int c = 0; c < kRc; c++)
-            if (c < nrhs) acc[c] = cadd(acc[c], cmul(dv[cc], yb[q * 16 + cc][c]));
+        for (int c = 0; c < NC; c++)
+            if (NC == 1 || c < nrhs) acc[c] = cadd(acc[c], cmul(dv[cc], yb[q * 16 + cc][c]));
     }
 #pragma unroll
-    for (int c = 0; c < kRc; c++) part[q][r][c] = acc[c];
+    for (int c = 0; c < NC; c++) part[q][r][c] = acc[c];
     __syncthreads();
     if (q == 0 && r < bs)
         for (int c = 0; c < nrhs; c++)
@@ -416,6 +416,28 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
 }
 
 // ------------------------------------------------------------------ host side
+template <typename C, bool LOWER>
+static void launch_chain_nc(int nc, int nb, cudaStream_t st, const C* LU, int n, const C* D, C* W, int64_t ldw,
+                            int* flags, unsigned* ticket, int epoch, DeviceStatus* dst) {
+    if (nc == 1)
+        k_trsv_chain<C, LOWER, 1><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+    else if (nc == 2)
+        k_trsv_chain<C, LOWER, 2><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+    else if (nc <= 4)
+        k_trsv_chain<C, LOWER, 4><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+    else
+        k_trsv_chain<C, LOWER, kRc><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+}
+
+template <typename C>
+static void launch_chain(bool lower, int nc, int nb, cudaStream_t st, const C* LU, int n, const C* D, C* W,
+                         int64_t ldw, int* flags, unsigned* ticket, int epoch, DeviceStatus* dst) {
+    if (lower)
+        launch_chain_nc<C, true>(nc, nb, st, LU, n, D, W, ldw, flags, ticket, epoch, dst);
+    else
+        launch_chain_nc<C, false>(nc, nb, st, LU, n, D, W, ldw, flags, ticket, epoch, dst);
+}
+
 struct TrsvWs {
     void* dinv = nullptr;      // Linv blocks then Uinv blocks
     int* flags = nullptr;
@@ -453,12 +475,8 @@ int trsv_solve(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_buf
         for (int pass = 0; pass < 2; pass++) {
             int epoch = ++ctx->trsv_epoch;
             if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream), "ticket"))) return rc;
-            if (pass == 0)
-                k_trsv_chain<C, true><<<nb, 256, 0, ctx->stream>>>(LU, n, n, Linv, W + c0 * ldw, ldw, nc, flags,
-                                                                   ticket, epoch, dst);
-            else
-                k_trsv_chain<C, false><<<nb, 256, 0, ctx->stream>>>(LU, n, n, Uinv, W + c0 * ldw, ldw, nc, flags,
-                                                                    ticket, epoch, dst);
+            launch_chain<C>(pass == 0, nc, nb, ctx->stream, LU, n, pass == 0 ? Linv : Uinv, W + c0 * ldw, ldw, flags,
+                            ticket, epoch, dst);
             count_launch(ctx);
         }
     }
