@@ -215,7 +215,20 @@ bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
 // previous call with the same L, m, k.
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                    const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev,
-                   int accumulate = 1, int max_ctas = 0, int reuse_a = 0);   // gemm_tc.cu
+                   int accumulate = 1, int max_ctas = 0, int reuse_a = 0);
+// Operands of the no-pivot LU's trailing updates written by tc_lu_panel (gemm_tc.cu).
+struct TcPanel {
+    float* Lah;
+    float* Lal;
+    float* Ubh;
+    float* Ubl;
+    int rest, KP;
+};
+size_t tc_panel_ws_bytes(int64_t n);
+int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, const float2* Uinv,
+                const float2* Linv, TcPanel* out);
+int tc_lu_update(frico_gpu_ctx* ctx, const TcPanel& pn, float2* C, int64_t ldc, int boff, int ncols, int max_ctas,
+                 cudaEvent_t* ev);   // gemm_tc.cu
 int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                        const float2* U, int64_t ldu, int m, int n, int k);  // lu.cu
 int trsm_lower_unit_f32(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int cb, int ce);  // lu.cu

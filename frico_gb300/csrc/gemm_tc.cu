@@ -55,7 +55,8 @@ template <int BN> struct Cfg {
     static constexpr int B_TILE = BN * BK * 4;
     static constexpr int STAGES = BN == 128 ? 3 : 2;
     static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr int STAGING = 8 * 32 * 32 * 4;   // per epilogue warp a 32 x 32 float block (A* emission)
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGING + 1024 + 256;
     static constexpr int TMEM_COLS = 2 * BN;
 };
 
@@ -147,19 +148,36 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-struct GemmArgs {
+// One problem of a launch. emit: the finished values of C also go, split into
+// hi/lo TF32, to the operand layout of a later update: 1 = as its A* (rows of
+// this C, K = this C's columns), 2 = as its B^ (row j = column j of this C).
+struct GemmProb {
     float* C;          // real view of the complex C: M x N column-major, ld = ldc floats
     int64_t ldc;
-    int M, N, KP;      // KP = padded K in floats (multiple of 32)
+    int M, N;          // real rows (2 x complex rows), columns
+    int tiles_m, tiles;
     int accumulate;    // 1: C -= A B; 0: C = A B
+    int emit;          // 0, 1 (A*) or 2 (B^), into eh / el with rows of KP floats
+    float* eh;
+    float* el;
+};
+
+// Up to two independent problems in one launch (tiles of problem 0, then 1),
+// with the same padded K. KP = padded K in floats (multiple of 32).
+struct GemmArgs {
+    GemmProb p[2];
+    int nprob, KP;
     DeviceStatus* st;
 };
 
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
 template <int BN>
-__global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(const __grid_constant__ CUtensorMap tmAh,
-                                                        const __grid_constant__ CUtensorMap tmAl,
-                                                        const __grid_constant__ CUtensorMap tmBh,
-                                                        const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
+__global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
+    const __grid_constant__ CUtensorMap tmAh0, const __grid_constant__ CUtensorMap tmAl0,
+    const __grid_constant__ CUtensorMap tmBh0, const __grid_constant__ CUtensorMap tmBl0,
+    const __grid_constant__ CUtensorMap tmAh1, const __grid_constant__ CUtensorMap tmAl1,
+    const __grid_constant__ CUtensorMap tmBh1, const __grid_constant__ CUtensorMap tmBl1, GemmArgs g) {
     constexpr int STAGES = Cfg<BN>::STAGES, STAGE_BYTES = Cfg<BN>::STAGE_BYTES;
     constexpr int A_TILE = Cfg<BN>::A_TILE, B_TILE = Cfg<BN>::B_TILE, TMEM_COLS = Cfg<BN>::TMEM_COLS;
     static_assert(BN == 2 * 64, "the epilogue gives each of two warps per quadrant 64 columns");
@@ -172,10 +190,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(const __grid_consta
     uint64_t* tfull = bars + 2 * STAGES;   // [2]
     uint64_t* tempty = bars + 2 * STAGES + 2;  // [2]
     uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 4);
+    float* staging = (float*)(ring + STAGES * STAGE_BYTES + 256);   // 8 x 32 x 32 floats
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tiles_m = (g.M + BM - 1) / BM, tiles_n = (g.N + BN - 1) / BN;
-    const int ntiles = tiles_m * tiles_n;
+    const int ntiles = g.p[0].tiles + (g.nprob > 1 ? g.p[1].tiles : 0);
     const int kslabs = g.KP / BK;
 
     if (threadIdx.x == 0) {
@@ -204,16 +222,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(const __grid_consta
             int it = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int mt = t % tiles_m, nt_ = t / tiles_m;
+                const int pi = t >= g.p[0].tiles ? 1 : 0;
+                const int tt = t - (pi ? g.p[0].tiles : 0), tm = pi ? g.p[1].tiles_m : g.p[0].tiles_m;
+                const int mt = tt % tm, nt_ = tt / tm;
+                const CUtensorMap* mAh = pi ? &tmAh1 : &tmAh0;
+                const CUtensorMap* mAl = pi ? &tmAl1 : &tmAl0;
+                const CUtensorMap* mBh = pi ? &tmBh1 : &tmBh0;
+                const CUtensorMap* mBl = pi ? &tmBl1 : &tmBl0;
                 for (int ks = 0; ks < kslabs; ks++, it++) {
                     const int s = it % STAGES, round = it / STAGES;
                     if (!(ok = mbar_wait(&empty[s], (round & 1) ^ 1, g.st))) break;
                     unsigned char* base = ring + s * STAGE_BYTES;
                     mbar_expect_tx(&full[s], STAGE_BYTES);
-                    tma_load_2d(base, &tmAh, &full[s], ks * BK, mt * BM);
-                    tma_load_2d(base + A_TILE, &tmAl, &full[s], ks * BK, mt * BM);
-                    tma_load_2d(base + 2 * A_TILE, &tmBh, &full[s], ks * BK, nt_ * BN);
-                    tma_load_2d(base + 2 * A_TILE + B_TILE, &tmBl, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base, mAh, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + A_TILE, mAl, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + 2 * A_TILE, mBh, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base + 2 * A_TILE + B_TILE, mBl, &full[s], ks * BK, nt_ * BN);
                 }
             }
         }
@@ -257,19 +281,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(const __grid_consta
         int tcount = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, tcount++) {
             const int acc = tcount & 1, around = tcount >> 1;
-            const int mt = t % tiles_m, nt_ = t / tiles_m;
+            const int pi = t >= g.p[0].tiles ? 1 : 0;
+            const GemmProb P = pi ? g.p[1] : g.p[0];
+            const int tt = t - (pi ? g.p[0].tiles : 0);
+            const int mt = tt % P.tiles_m, nt_ = tt / P.tiles_m;
             const int gr = mt * BM + row;
-            const int ncol = min(64, g.N - nt_ * BN - h);   // columns of this warp's half (may be <= 0)
-            const bool rowok = gr < g.M;
-            float* cp = g.C + int64_t(nt_ * BN + h) * g.ldc + gr;
+            const int ncol = min(64, P.N - nt_ * BN - h);   // columns of this warp's half (may be <= 0)
+            const bool rowok = gr < P.M;
+            const int64_t ldc = P.ldc;
+            const int accumulate = P.accumulate, emit = P.emit;
+            float* cp = P.C + int64_t(nt_ * BN + h) * ldc + gr;
             // C values first: these reads do not depend on the accumulator
             float cv[64];
-            if (g.accumulate && rowok && ncol == 64) {
+            if (accumulate && rowok && ncol == 64) {
 #pragma unroll
-                for (int j = 0; j < 64; j++) cv[j] = cp[int64_t(j) * g.ldc];
+                for (int j = 0; j < 64; j++) cv[j] = cp[int64_t(j) * ldc];
             } else {
 #pragma unroll
-                for (int j = 0; j < 64; j++) cv[j] = (g.accumulate && rowok && j < ncol) ? cp[int64_t(j) * g.ldc] : 0.f;
+                for (int j = 0; j < 64; j++) cv[j] = (accumulate && rowok && j < ncol) ? cp[int64_t(j) * ldc] : 0.f;
             }
             if (!mbar_wait(&tfull[acc], around & 1, g.st)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -282,10 +311,41 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(const __grid_consta
             for (int c0 = 0; c0 < 64; c0 += 32) {
                 float v[32];
                 tmem_ld32(taddr + uint32_t(c0), v);
-                float* wp = sp + int64_t(c0) * g.ldc;
+                float* wp = sp + int64_t(c0) * ldc;
+                float* stg = staging + (warp - 2) * 1024;   // [row (lane)][column ^ row], 32 x 32
 #pragma unroll
-                for (int j = 0; j < 32; j++)
-                    if (rowok && c0 + j < ncol) wp[int64_t(j) * g.ldc] = g.accumulate ? cv[c0 + j] - v[j] : v[j];
+                for (int j = 0; j < 32; j++) {
+                    const float o = accumulate ? cv[c0 + j] - v[j] : v[j];
+                    const bool ok = rowok && c0 + j < ncol;
+                    if (ok) wp[int64_t(j) * ldc] = o;
+                    if (emit == 1) {
+                        stg[lane * 32 + (j ^ lane)] = o;
+                    } else if (emit == 2 && ok) {
+                        const int64_t off = int64_t(nt_ * BN + h + c0 + j) * g.KP + gr;
+                        const float hi = tf32_hi(o);
+                        P.eh[off] = hi;
+                        P.el[off] = o - hi;
+                    }
+                }
+                if (emit == 1) {
+                    // A* row R: (re, -im) (R = 2 r) or (im, re) (R = 2 r + 1) at K = 2 col, 2 col + 1.
+                    // Read back transposed, lane = column: each store covers 256 contiguous bytes of a row.
+                    __syncwarp();
+                    const int col = nt_ * BN + h + c0 + lane;
+                    const bool colok = c0 + lane < ncol;
+                    for (int i = 0; i < 32; i++) {
+                        const int R = mt * BM + q * 32 + i;
+                        const float a = stg[i * 32 + (lane ^ i)], b = stg[(i ^ 1) * 32 + (lane ^ (i ^ 1))];
+                        if (colok && R < P.M) {
+                            const float2 w = (i & 1) ? make_float2(a, b) : make_float2(a, -b);
+                            const int64_t off = int64_t(R) * g.KP + 2 * col;
+                            const float2 wh = make_float2(tf32_hi(w.x), tf32_hi(w.y));
+                            *reinterpret_cast<float2*>(P.eh + off) = wh;
+                            *reinterpret_cast<float2*>(P.el + off) = make_float2(w.x - wh.x, w.y - wh.y);
+                        }
+                    }
+                    __syncwarp();
+                }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -346,20 +406,34 @@ __device__ __forceinline__ void split_b_elem(int64_t idx, const float2* __restri
     Bl[idx] = x - hi;
 }
 
-// Both operand splits of one update in a single launch: blocks [0, nA) split A
-// (32 rows x 64-column chunks of K, a_cols chunks per row band), the rest
-// split B (256 floats each). nA = 0 when the A split is reused.
-__global__ void __launch_bounds__(256) k_split_ab(const float2* __restrict__ L, int64_t ldl, int m, int k, int KP,
-                                                 float* __restrict__ Ah, float* __restrict__ Al, int nA, int a_cols,
-                                                 const float2* __restrict__ U, int64_t ldu, int n,
-                                                 float* __restrict__ Bh, float* __restrict__ Bl) {
+// Operand splits of one or two updates in a single launch: up to four parts,
+// each an A* (32-row bands x 64-column chunks of K, a_cols chunks per band) or
+// a B^ (256 floats per block) split; blocks are numbered part after part.
+struct SplitPart {
+    const float2* src;
+    int64_t ld;
+    int rows, k;       // A*: complex rows m; B^: columns n. k: complex K
+    float* hi;
+    float* lo;
+    int isB, a_cols, blocks;
+};
+struct SplitArgs {
+    SplitPart p[4];
+    int np, KP;
+};
+
+__global__ void __launch_bounds__(256) k_split_parts(SplitArgs a) {
     __shared__ float2 t[32][65];
-    const int b = blockIdx.x;
-    if (b < nA) {
-        split_a_tile(b / a_cols, b % a_cols, L, ldl, m, k, KP, Ah, Al, t);
-    } else {
-        split_b_elem(int64_t(b - nA) * blockDim.x + threadIdx.x, U, ldu, k, n, KP, Bh, Bl);
+    int b = blockIdx.x, i = 0;
+    while (i + 1 < a.np && b >= (i == 0 ? a.p[0].blocks : i == 1 ? a.p[1].blocks : a.p[2].blocks)) {
+        b -= i == 0 ? a.p[0].blocks : i == 1 ? a.p[1].blocks : a.p[2].blocks;
+        i++;
     }
+    const SplitPart P = i == 0 ? a.p[0] : i == 1 ? a.p[1] : i == 2 ? a.p[2] : a.p[3];
+    if (P.isB)
+        split_b_elem(int64_t(b) * blockDim.x + threadIdx.x, P.src, P.ld, P.k, P.rows, a.KP, P.hi, P.lo);
+    else
+        split_a_tile(b / P.a_cols, b % P.a_cols, P.src, P.ld, P.rows, P.k, a.KP, P.hi, P.lo, t);
 }
 
 }  // namespace tc
@@ -403,6 +477,91 @@ bool gemm_tc_available(frico_gpu_ctx* ctx) {
     return major == 10 && minor == 3 && encode_fn() != nullptr;
 }
 
+static tc::SplitPart split_part(bool isB, const float2* src, int64_t ld, int rows, int k, float* hi, float* lo,
+                                int KP) {
+    tc::SplitPart p;
+    p.src = src;
+    p.ld = ld;
+    p.rows = rows;
+    p.k = k;
+    p.hi = hi;
+    p.lo = lo;
+    p.isB = isB ? 1 : 0;
+    p.a_cols = (KP / 2 + 63) / 64;
+    p.blocks = isB ? int((int64_t(rows) * KP + 255) / 256) : ((rows + 31) / 32) * p.a_cols;
+    return p;
+}
+
+static int launch_split(frico_gpu_ctx* ctx, cudaStream_t st, const tc::SplitPart* parts, int np, int KP) {
+    tc::SplitArgs a;
+    int blocks = 0;
+    for (int i = 0; i < 4; i++) {
+        a.p[i] = parts[i < np ? i : np - 1];
+        if (i < np) blocks += parts[i].blocks;
+    }
+    a.np = np;
+    a.KP = KP;
+    if (blocks == 0) return FRICO_GPU_OK;
+    tc::k_split_parts<<<unsigned(blocks), 256, 0, st>>>(a);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_split_parts");
+}
+
+// One problem of a launch: its four tensor maps (A* hi/lo with a_rows rows, B^
+// hi/lo with b_rows rows, KP floats each) and its C.
+struct TcProblem {
+    CUtensorMap mah, mal, mbh, mbl;
+    tc::GemmProb p;
+};
+
+static int make_problem(frico_gpu_ctx* ctx, TcProblem& q, float2* C, int64_t ldc, int M, int N, const float* Ah,
+                        const float* Al, const float* Bh, const float* Bl, int KP, int accumulate, int emit,
+                        float* eh, float* el) {
+    if (!make_map(&q.mah, (float*)Ah, M, KP, tc::BM) || !make_map(&q.mal, (float*)Al, M, KP, tc::BM) ||
+        !make_map(&q.mbh, (float*)Bh, N, KP, 128) || !make_map(&q.mbl, (float*)Bl, N, KP, 128))
+        return set_err(ctx, FRICO_GPU_ECUDA, "cuTensorMapEncodeTiled failed");
+    q.p.C = (float*)C;
+    q.p.ldc = 2 * ldc;
+    q.p.M = M;
+    q.p.N = N;
+    q.p.tiles_m = (M + tc::BM - 1) / tc::BM;
+    q.p.tiles = q.p.tiles_m * ((N + 127) / 128);
+    q.p.accumulate = accumulate;
+    q.p.emit = emit;
+    q.p.eh = eh;
+    q.p.el = el;
+    return FRICO_GPU_OK;
+}
+
+static int launch_gemm(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem* q, int np, int KP, int max_ctas,
+                       cudaEvent_t* ev) {
+    int rc;
+    if ((rc = device_once(ctx, kOnceGemmTc, [](frico_gpu_ctx* c) {
+             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3<128>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       tc::Cfg<128>::SMEM_BYTES), "tc smem attribute");
+         })))
+        return rc;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    tc::GemmArgs ga;
+    ga.p[0] = q[0].p;
+    ga.p[1] = q[np > 1 ? 1 : 0].p;
+    ga.nprob = np;
+    ga.KP = KP;
+    ga.st = (DeviceStatus*)ctx->status.p;
+    const int ntiles = q[0].p.tiles + (np > 1 ? q[1].p.tiles : 0);
+    if (ntiles == 0) return FRICO_GPU_OK;
+    const TcProblem& q1 = q[np > 1 ? 1 : 0];
+    if (ev) cudaEventRecord(ev[0], st);
+    const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
+    tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(
+        q[0].mah, q[0].mal, q[0].mbh, q[0].mbl, q1.mah, q1.mal, q1.mbh, q1.mbl, ga);
+    if (ev) cudaEventRecord(ev[1], st);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");
+}
+
 // C[m x n] -= L[m x k] * U[k x n] (accumulate = 1) or C = L U (accumulate = 0),
 // complex64 column-major, leading dims ldc, ldl, ldu. C may alias L or U: both
 // operands are copied (split) before the MMA kernel writes C.
@@ -421,44 +580,75 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
     float* Bh = Al + a_elems;
     float* Bl = Bh + b_elems;
     cudaStream_t st = ctx->stream;
-    {
-        const int a_cols = (KP / 2 + 63) / 64;
-        const int nA = reuse_a ? 0 : ((m + 31) / 32) * a_cols;
-        const int nB = int((b_elems + 255) / 256);
-        tc::k_split_ab<<<unsigned(nA + nB), 256, 0, st>>>(L, ldl, m, k, KP, Ah, Al, nA, a_cols, U, ldu, n, Bh, Bl);
-        count_launch(ctx);
-    }
-    // 128-column tiles: 256-column tiles (two stages, 25% fewer operand bytes from L2 per
-    // output) measured no faster on the LU's updates (N = 7680: 463 vs 464 TFLOP/s)
-    const int BNsel = 128;
-    CUtensorMap mah, mal, mbh, mbl;
-    if (!make_map(&mah, Ah, M, KP, tc::BM) || !make_map(&mal, Al, M, KP, tc::BM) ||
-        !make_map(&mbh, Bh, n, KP, BNsel) || !make_map(&mbl, Bl, n, KP, BNsel))
-        return set_err(ctx, FRICO_GPU_ECUDA, "cuTensorMapEncodeTiled failed");
-    if ((rc = device_once(ctx, kOnceGemmTc, [](frico_gpu_ctx* c) {
-             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3<128>,
-                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       tc::Cfg<128>::SMEM_BYTES), "tc smem attribute");
-         })))
+    tc::SplitPart parts[2];
+    int np = 0;
+    if (!reuse_a) parts[np++] = split_part(false, L, ldl, m, k, Ah, Al, KP);
+    parts[np++] = split_part(true, U, ldu, n, k, Bh, Bl, KP);
+    if ((rc = launch_split(ctx, st, parts, np, KP))) return rc;
+    TcProblem q;
+    if ((rc = make_problem(ctx, q, C, ldc, M, n, Ah, Al, Bh, Bl, KP, accumulate, 0, nullptr, nullptr))) return rc;
+    return launch_gemm(ctx, st, &q, 1, KP, max_ctas, ev);
+}
+
+// ---- the no-pivot LU's block column in three launches (see lu_nopiv.cu)
+static const int kPanelKP = 256;   // K = 128 complex columns
+
+static size_t al1k(size_t floats) { return (floats + 255) & ~size_t(255); }   // keep slots 1 KB aligned
+
+size_t tc_panel_ws_bytes(int64_t n) {
+    const size_t r = size_t(std::max<int64_t>(n - 128, 0)), KP = kPanelKP;
+    // A21 (A*), Uinv (B^), Linv (A*), A12 (B^), L21 (A*), U12 (B^): hi and lo each
+    return sizeof(float) * 2 * (2 * al1k(2 * r * KP) + 2 * al1k(r * KP) + al1k(128 * KP) + al1k(256 * KP)) + 4096;
+}
+
+// L21 = A21 U11^{-1} and U12 = L11^{-1} A12 (in place in A, jb = 128 columns /
+// rows, rest = rows of A21 = columns of A12) as one launch after one split
+// launch; their epilogues also write L21 as the A* and U12 as the B^ operand of
+// the block column's trailing updates (tc_lu_update).
+int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, const float2* Uinv,
+                const float2* Linv, TcPanel* out) {
+    const int KP = kPanelKP;
+    if (jb != 128 || rest <= 0) return set_err(ctx, FRICO_GPU_EINVAL, "tc_lu_panel: block of 128 expected");
+    int rc;
+    if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
+    const size_t r = size_t(rest);
+    float* base = (float*)(((uintptr_t)ctx->tc_ws.p + 1023) & ~uintptr_t(1023));
+    auto take = [&](size_t floats) { float* p = base; base += al1k(floats); return p; };
+    float* a21h = take(2 * r * KP); float* a21l = take(2 * r * KP);
+    float* uih = take(128 * KP);    float* uil = take(128 * KP);
+    float* lih = take(256 * KP);    float* lil = take(256 * KP);
+    float* a12h = take(r * KP);     float* a12l = take(r * KP);
+    out->Lah = take(2 * r * KP);    out->Lal = take(2 * r * KP);
+    out->Ubh = take(r * KP);        out->Ubl = take(r * KP);
+    out->rest = rest;
+    out->KP = KP;
+    cudaStream_t st = ctx->stream;
+    float2* A21 = A + int64_t(k0) * lda + k0 + jb;
+    float2* A12 = A + int64_t(k0 + jb) * lda + k0;
+    const tc::SplitPart parts[4] = {split_part(false, A21, lda, rest, jb, a21h, a21l, KP),
+                                    split_part(true, Uinv, 128, jb, jb, uih, uil, KP),
+                                    split_part(false, Linv, 128, jb, jb, lih, lil, KP),
+                                    split_part(true, A12, lda, rest, jb, a12h, a12l, KP)};
+    if ((rc = launch_split(ctx, st, parts, 4, KP))) return rc;
+    TcProblem q[2];
+    if ((rc = make_problem(ctx, q[0], A21, lda, 2 * rest, jb, a21h, a21l, uih, uil, KP, 0, 1, out->Lah, out->Lal)))
         return rc;
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const int ntiles = ((M + tc::BM - 1) / tc::BM) * ((n + BNsel - 1) / BNsel);
-    tc::GemmArgs ga;
-    ga.C = (float*)C;
-    ga.ldc = 2 * ldc;
-    ga.M = M;
-    ga.N = n;
-    ga.KP = KP;
-    ga.accumulate = accumulate;
-    ga.st = (DeviceStatus*)ctx->status.p;
-    if (ev) cudaEventRecord(ev[0], st);
-    const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
-    tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(mah, mal, mbh, mbl,
-                                                                                                  ga);
-    if (ev) cudaEventRecord(ev[1], st);
-    count_launch(ctx);
-    return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");
+    if ((rc = make_problem(ctx, q[1], A12, lda, 2 * jb, rest, lih, lil, a12h, a12l, KP, 0, 2, out->Ubh, out->Ubl)))
+        return rc;
+    return launch_gemm(ctx, st, q, 2, KP, 0, nullptr);
+}
+
+// C[rest x ncols] -= L21 U12[:, boff : boff + ncols] from the operands tc_lu_panel wrote.
+int tc_lu_update(frico_gpu_ctx* ctx, const TcPanel& pn, float2* C, int64_t ldc, int boff, int ncols, int max_ctas,
+                 cudaEvent_t* ev) {
+    if (ncols <= 0) return FRICO_GPU_OK;
+    const int KP = pn.KP;
+    TcProblem q;
+    int rc;
+    if ((rc = make_problem(ctx, q, C, ldc, 2 * pn.rest, ncols, pn.Lah, pn.Lal, pn.Ubh + int64_t(boff) * KP,
+                           pn.Ubl + int64_t(boff) * KP, KP, 1, 0, nullptr, nullptr)))
+        return rc;
+    return launch_gemm(ctx, ctx->stream, &q, 1, KP, max_ctas, ev);
 }
 
 }  // namespace frico

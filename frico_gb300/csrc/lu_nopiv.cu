@@ -472,11 +472,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     if (tc) {
         // every buffer the factorisation touches is sized before the first launch, so that
         // the launch sequence can be captured once and replayed as a CUDA graph
-        {
-            const int64_t rest0 = std::max(0, n - kNP);
-            const size_t a_el = size_t(2 * rest0) * 256, b_el = size_t(std::max<int64_t>(rest0, kNP)) * 256;
-            if ((rc = ensure(ctx, ctx->tc_ws, sizeof(float) * 2 * (a_el + b_el) + 4096))) return rc;
-        }
+        if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(n)))) return rc;
         if ((rc = lookahead_streams(ctx))) return rc;
         auto enqueue = [&]() -> int {
             int rc = cuda_check(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(DeviceStatus), st), "status");
@@ -495,11 +491,10 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                 const int rest = n - k0 - jb;
                 if (diag_on_s2 && (rc = cuda_check(ctx, cudaStreamWaitEvent(st, ev_diag, 0), "wait diag"))) return rc;
                 if (rest == 0) break;
-                C* A21 = A + int64_t(k0) * lda + k0 + jb;
-                C* A12 = A + int64_t(k0 + jb) * lda + k0;
-                // L21 = A21 U11^{-1},  U12 = L11^{-1} A12 on the tensor cores (overwrite mode)
-                if ((rc = gemm_update_tc(ctx, A21, lda, A21, lda, Uinv_of(k0), kNP, rest, jb, jb, nullptr, 0))) return rc;
-                if ((rc = gemm_update_tc(ctx, A12, lda, Linv_of(k0), kNP, A12, lda, jb, rest, jb, nullptr, 0))) return rc;
+                // L21 = A21 U11^{-1}, U12 = L11^{-1} A12 on the tensor cores, one launch that
+                // also writes both as the operands of the updates below
+                TcPanel pn;
+                if ((rc = tc_lu_panel(ctx, A, lda, k0, jb, rest, Uinv_of(k0), Linv_of(k0), &pn))) return rc;
                 // trailing update, next block column first; that block's LU then runs on the
                 // second stream while the rest of the update (on all but two SMs) proceeds
                 const int jb1 = std::min(kNP, rest);
@@ -509,7 +504,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                     ctx->stats.gemm_flops += 8.0 * double(rest) * double(jb1) * double(jb);
                     ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(jb1) + double(rest) * jb + double(jb) * jb1);
                 }
-                if ((rc = gemm_update_tc(ctx, Cm, lda, A21, lda, A12, lda, rest, jb1, jb, ev))) return rc;
+                if ((rc = tc_lu_update(ctx, pn, Cm, lda, 0, jb1, 0, ev))) return rc;
                 if ((rc = cuda_check(ctx, cudaEventRecord(ev_narrow, st), "record"))) return rc;
                 if ((rc = cuda_check(ctx, cudaStreamWaitEvent(s2, ev_narrow, 0), "wait narrow"))) return rc;
                 if ((rc = launch_diag_lu(ctx, s2, A, lda, k0 + jb, jb1, Uinv_of(k0 + jb), Linv_of(k0 + jb), Blk, dst)))
@@ -523,8 +518,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                         ctx->stats.gemm_flops += 8.0 * double(rest) * double(nr) * double(jb);
                         ctx->stats.gemm_bytes += sizeof(C) * (2.0 * double(rest) * double(nr) + double(jb) * nr);
                     }
-                    if ((rc = gemm_update_tc(ctx, Cm + int64_t(jb1) * lda, lda, A21, lda, A12 + int64_t(jb1) * lda, lda,
-                                             rest, nr, jb, ev, 1, std::max(1, sms - 2), 1)))
+                    if ((rc = tc_lu_update(ctx, pn, Cm + int64_t(jb1) * lda, lda, jb1, nr, std::max(1, sms - 2), ev)))
                         return rc;
                 }
                 if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
