@@ -127,6 +127,19 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def gemm_traffic_per_launch(level: int, precision: str):
+    """DRAM bytes per narrow / trailing-update launch of the complex64 LU from one
+    ncu capture (dram__bytes_read.sum + dram__bytes_write.sum over all of a
+    solve's update launches), recorded with its command in
+    profiles/k_gemm_tf32x3_sphere_L4_mixed.md; None for other configurations."""
+    p = ROOT / "profiles" / "k_gemm_tf32x3_sphere_L4_mixed.md"
+    if level != 4 or precision != "mixed" or not p.exists():
+        return None
+    import re
+    m = re.search(r"traffic_bytes_per_launch = ([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
 # ------------------------------------------------------------------ CPU paths
 def cpu_sample(mesh, steps: int, warmup: int, Zfull=None):
     """FRICO's CPU path on a bounded sample; returns (sec/solve list, cores, sample desc)."""
@@ -324,7 +337,9 @@ def run_ours(args):
         roof = {"bound": "tensor", "achieved": tensor_ach, "peak": tensor_peak, "unit": "TFLOP/s", "frac": frac_t}
     else:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": frac_m}
-    roof.update({"traffic": None,
+    roof.update({"traffic": gemm_traffic_per_launch(args.level, args.precision) if tc else None,
+                 "traffic_unit": "bytes per launch (ncu, DRAM read + write)",
+                 "algorithmic_bytes_per_launch": gby / max(1, gl),
                  "kernel": ("tc::k_gemm_tf32x3" if tc else "k_gemm_update<float>") if args.precision == "mixed"
                  else "k_gemm_update<double>",
                  "launches_per_step": gl / 2, "avg_launch_us": 1000.0 * gms / max(1, gl),

@@ -49,6 +49,57 @@ template <typename C> __host__ __device__ __forceinline__ C cdiv(C a, C b) {
 }
 template <typename C> __host__ __device__ __forceinline__ auto cabs1(C a) { return fabs(a.x) + fabs(a.y); }
 
+// ---------------------------------------------------------------- double-float
+// FP64 work on the FP32 pipe (many times wider than the FP64 one on this part):
+// a value is an unevaluated sum hi + lo of two FP32 numbers (about 47 bits).
+// split_df: FP64 d -> h + l by integer operations, |d - h - l| <= 2^-47 |d|;
+// zero and subnormal d give 0 + 0, exponents outside [-100, 127] set bad.
+__device__ __forceinline__ void split_df(double d, float& h, float& l, int& bad) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const unsigned hi = unsigned(u >> 32), lo = unsigned(u);
+    const unsigned sg = hi & 0x80000000u;
+    const int e = int((hi >> 20) & 0x7FFu);
+    const int E = e - 1023;
+    const bool zero = e == 0;   // zero or subnormal (below 1e-307): taken as zero
+    bad |= (!zero && (E < -100 || E > 127)) ? 1 : 0;
+    const int Ec = min(max(E, -100), 127);
+    const unsigned mtop = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned b = sg | (unsigned(Ec + 104) << 23);   // 2^(E-23), sign of d
+    const float hv = __uint_as_float(sg | (unsigned(Ec + 127) << 23) | mtop);
+    const float lv = __fsub_rn(__uint_as_float(b | ((lo & 0x1FFFFFFFu) >> 6)), __uint_as_float(b));
+    h = zero ? 0.f : hv;
+    l = zero ? 0.f : lv;
+}
+
+// (s, t) += a b, a = a1 + a2, b = b1 + b2
+__device__ __forceinline__ void df_mac(float& s, float& t, float a1, float a2, float b1, float b2) {
+    const float p = __fmul_rn(a1, b1);
+    float e = __fmaf_rn(a1, b1, -p);
+    e = __fmaf_rn(a1, b2, e);
+    e = __fmaf_rn(a2, b1, e);
+    const float sn = __fadd_rn(s, p);
+    const float v = __fsub_rn(sn, s);
+    t = __fadd_rn(t, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(sn, v)), __fsub_rn(p, v)), e));
+    s = sn;
+}
+
+__device__ __forceinline__ void df_renorm(float& s, float& t) {
+    const float sn = __fadd_rn(s, t);
+    t = __fsub_rn(t, __fsub_rn(sn, s));
+    s = sn;
+}
+
+// FP32 value as FP64 by integer operations (normal numbers; subnormals and zero give 0)
+__device__ __forceinline__ double f2d_exact(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0) return 0.0;
+    const unsigned long long b = (unsigned long long)(u & 0x80000000u) << 32 |
+                                 (unsigned long long)(e - 127u + 1023u) << 52 |
+                                 (unsigned long long)(u & 0x7FFFFFu) << 29;
+    return __longlong_as_double((long long)b);
+}
+
 // ---------------------------------------------------------------- errors
 #define FRICO_DEV_ERR_TIMEOUT 1
 #define FRICO_DEV_ERR_BOUNDS 2

@@ -140,9 +140,19 @@ struct BasisAsm {
     double hs_m, hs_p, hk_m, hk_p;
 };
 
+// The signed factors of the mode-0 assembly as double-float pairs (hi, lo), for
+// the assembly on the FP32 pipe; bad: some factor is outside the split's range,
+// and the entries of this RWG take the FP64 path.
+struct BasisDF {
+    int32_t itm, itp;
+    float um[3][2], up[3][2];
+    float hsm[2], hsp[2], hkm[2], hkp[2];
+    int32_t bad;
+};
+
 __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo,
                             const double* __restrict__ qp, int nq, int mode, double inv_ksq,
-                            BasisAsm* __restrict__ out) {
+                            BasisAsm* __restrict__ out, BasisDF* __restrict__ dfo) {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= n) return;
     BasisAsm b;
@@ -178,6 +188,20 @@ __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo
         b.u_p[d] = b.hs_p * b.a_p[d];
     }
     out[i] = b;
+    BasisDF f;
+    int bad = 0;
+    f.itm = b.itm;
+    f.itp = b.itp;
+    for (int d = 0; d < 3; d++) {
+        split_df(b.u_m[d], f.um[d][0], f.um[d][1], bad);
+        split_df(b.u_p[d], f.up[d][0], f.up[d][1], bad);
+    }
+    split_df(b.hs_m, f.hsm[0], f.hsm[1], bad);
+    split_df(b.hs_p, f.hsp[0], f.hsp[1], bad);
+    split_df(b.hk_m, f.hkm[0], f.hkm[1], bad);
+    split_df(b.hk_p, f.hkp[0], f.hkp[1], bad);
+    f.bad = bad;
+    dfo[i] = f;
 }
 
 // ------------------------------------------------------------------ phase 1
@@ -356,6 +380,7 @@ struct AsmArgs {
     int64_t n, nt, ldz;
     double inv_ksq;
     const BasisAsm* bas;
+    const BasisDF* bdf;  // the same, double-float (mode 0)
     const double2* G;    // mode 0/2: [nt*nt]; mode 1: 8 planes
     const double2* S;    // split moments [n*4*8]
     double2* Z64;        // may be null
@@ -483,11 +508,52 @@ __device__ __forceinline__ double2 entry_mode0(const AsmArgs& A, const BasisAsm&
     return entry;
 }
 
+// One mode-0 entry in double-float for RWGs that share no triangle (all four
+// blocks are table blocks): sum over the blocks of g_ab f_ab with
+// f_ab = u_ia . u_jb + hk_ia hs_jb, the same terms as entry_mode0. Returns
+// false when a table value is outside the split's range (the caller then takes
+// the FP64 path); (er, ei) = the entry as (hi, lo) pairs.
+__device__ __forceinline__ bool entry_mode0_df(const AsmArgs& A, const BasisDF& di, const BasisDF& dj, float2& er,
+                                               float2& ei) {
+    float rs = 0.f, rt = 0.f, is = 0.f, it = 0.f;
+    int bad = 0;
+#pragma unroll
+    for (int blk = 0; blk < 4; blk++) {
+        const int s = blk >> 1, t = blk & 1;
+        const int32_t ta = s ? di.itp : di.itm;
+        const int32_t tb = t ? dj.itp : dj.itm;
+        const float(*ui)[2] = s ? di.up : di.um;
+        const float(*uj)[2] = t ? dj.up : dj.um;
+        const float* hk = s ? di.hkp : di.hkm;
+        const float* hs = t ? dj.hsp : dj.hsm;
+        float fs = 0.f, ft = 0.f;
+        df_mac(fs, ft, ui[0][0], ui[0][1], uj[0][0], uj[0][1]);
+        df_mac(fs, ft, ui[1][0], ui[1][1], uj[1][0], uj[1][1]);
+        df_mac(fs, ft, ui[2][0], ui[2][1], uj[2][0], uj[2][1]);
+        df_mac(fs, ft, hk[0], hk[1], hs[0], hs[1]);
+        df_renorm(fs, ft);
+        const double2 g = A.G[int64_t(ta) * A.nt + tb];
+        float gx1, gx2, gy1, gy2;
+        split_df(g.x, gx1, gx2, bad);
+        split_df(g.y, gy1, gy2, bad);
+        df_mac(rs, rt, gx1, gx2, fs, ft);
+        df_mac(is, it, gy1, gy2, fs, ft);
+    }
+    df_renorm(rs, rt);
+    df_renorm(is, it);
+    er = make_float2(rs, rt);
+    ei = make_float2(is, it);
+    return bad == 0;
+}
+
 // Mode-0 assembly over the lower triangle of 32 x 32 tiles. Z[j, i] = Z[i, j]
 // whenever RWGs i and j share no triangle (no sub-triangle split on either side:
 // the Green table is symmetric and so is the block expression), so an
 // off-diagonal tile is computed once and also written transposed through shared
-// memory; the few pairs that share a triangle are computed in both orientations.
+// memory; the few pairs that share a triangle are computed in both orientations
+// in FP64 (entry_mode0). The others are computed in double-float on the FP32
+// pipe (entry_mode0_df; |error| about 2^-46 of sum |g f|), the FP64 value being
+// the exact sum hi + lo rounded once and the complex64 one hi + lo rounded in FP32.
 __global__ void __launch_bounds__(256) k_assemble_sym0(AsmArgs A) {
     const int64_t t = blockIdx.x;
     int J = int((sqrt(8.0 * double(t) + 1.0) - 1.0) * 0.5);
@@ -495,24 +561,41 @@ __global__ void __launch_bounds__(256) k_assemble_sym0(AsmArgs A) {
     while (int64_t(J + 1) * (J + 2) / 2 <= t) J++;
     const int I = int(t - int64_t(J) * (J + 1) / 2);   // I <= J
     __shared__ double2 tr[32][33];
+    __shared__ float2 tr32[32][33];
     const int jl = threadIdx.x & 31, il0 = threadIdx.x >> 5;
     const int64_t j = int64_t(J) * 32 + jl;
     const bool jok = j < A.n;
-    BasisAsm bj;
-    if (jok) bj = A.bas[j];
+    BasisDF dj;
+    if (jok) dj = A.bdf[j];
 #pragma unroll 1
     for (int kk = 0; kk < 4; kk++) {
         const int il = il0 + 8 * kk;
         const int64_t i = int64_t(I) * 32 + il;
         if (jok && i < A.n) {
-            const BasisAsm bi = A.bas[i];
-            const double2 e = entry_mode0(A, bi, bj, i);
+            const BasisDF di = A.bdf[i];
+            const bool shared = dj.itm == di.itm || dj.itm == di.itp || dj.itp == di.itm || dj.itp == di.itp;
+            double2 e;
+            float2 e32;
+            float2 er, ei;
+            if (!shared && !(di.bad | dj.bad) && entry_mode0_df(A, di, dj, er, ei)) {
+                e = make_double2(f2d_exact(er.x) + f2d_exact(er.y), f2d_exact(ei.x) + f2d_exact(ei.y));
+                e32 = make_float2(__fadd_rn(er.x, er.y), __fadd_rn(ei.x, ei.y));
+            } else {
+                e = entry_mode0(A, A.bas[i], A.bas[j], i);
+                e32 = make_float2(float(e.x), float(e.y));
+            }
             const int64_t o = i * A.ldz + j;
             if (A.Z64) A.Z64[o] = e;
-            if (A.Z32) A.Z32[o] = make_float2(float(e.x), float(e.y));
-            if (I != J) {
-                const bool shared = bj.itm == bi.itm || bj.itm == bi.itp || bj.itp == bi.itm || bj.itp == bi.itp;
-                tr[il][jl] = shared ? entry_mode0(A, bj, bi, j) : e;   // Z[i, j]
+            if (A.Z32) A.Z32[o] = e32;
+            if (I != J) {   // Z[i, j]
+                if (shared) {
+                    const double2 et = entry_mode0(A, A.bas[j], A.bas[i], j);
+                    tr[il][jl] = et;
+                    tr32[il][jl] = make_float2(float(et.x), float(et.y));
+                } else {
+                    tr[il][jl] = e;
+                    tr32[il][jl] = e32;
+                }
             }
         }
     }
@@ -523,10 +606,9 @@ __global__ void __launch_bounds__(256) k_assemble_sym0(AsmArgs A) {
         const int r = threadIdx.x & 31, c = (threadIdx.x >> 5) + 8 * kk;
         const int64_t i = int64_t(I) * 32 + r, jj = int64_t(J) * 32 + c;
         if (i < A.n && jj < A.n) {
-            const double2 e = tr[r][c];
             const int64_t o = jj * A.ldz + i;
-            if (A.Z64) A.Z64[o] = e;
-            if (A.Z32) A.Z32[o] = make_float2(float(e.x), float(e.y));
+            if (A.Z64) A.Z64[o] = tr[r][c];
+            if (A.Z32) A.Z32[o] = tr32[r][c];
         }
     }
 }
@@ -595,7 +677,8 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     const double k = omega * std::sqrt(FRICO_MU0 * FRICO_EPS0);
     const double inv_ksq = 1. / (omega * omega * FRICO_MU0 * FRICO_EPS0);
 
-    if ((rc = ensure(ctx, ctx->basis_aux, sizeof(BasisAsm) * n))) return rc;
+    if ((rc = ensure(ctx, ctx->basis_aux, (sizeof(BasisAsm) + sizeof(BasisDF)) * n + 256))) return rc;
+    BasisDF* bdf = (BasisDF*)(((uintptr_t)((BasisAsm*)ctx->basis_aux.p + n) + 255) & ~uintptr_t(255));
     const size_t gbytes = sizeof(double2) * size_t(nt) * size_t(nt) * (mode == 1 ? 8 : 1);
     if ((rc = ensure(ctx, ctx->gtab, gbytes))) return rc;
     if (mode != 2 && (rc = ensure(ctx, ctx->smom, sizeof(double2) * 32 * n))) return rc;
@@ -609,7 +692,7 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     const double* qps = (const double*)ctx->qps.p;
     cudaStream_t st = ctx->stream;
     k_basis_aux<<<unsigned((n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, nq, mode, inv_ksq,
-                                                           (BasisAsm*)ctx->basis_aux.p);
+                                                           (BasisAsm*)ctx->basis_aux.p, bdf);
     dim3 gt(unsigned((nt + 127) / 128), unsigned(nt));
     double2* G = (double2*)ctx->gtab.p;
     const int64_t T = (nt + 31) / 32;
@@ -630,6 +713,7 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     a.ldz = n;
     a.inv_ksq = inv_ksq;
     a.bas = (const BasisAsm*)ctx->basis_aux.p;
+    a.bdf = bdf;
     a.G = G;
     a.S = (const double2*)ctx->smom.p;
     a.Z64 = (double2*)ctx->z64.p;

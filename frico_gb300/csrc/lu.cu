@@ -544,41 +544,7 @@ __global__ void __launch_bounds__(256) k_residual_part(const double2* __restrict
 // over a flush block (FP64 summation: 2^-53 per term).
 // An exponent outside [-100, 127] (values beyond about 1e-30 .. 3e38, or not
 // finite) sets st->df_range; the caller then recomputes with k_residual_part.
-__device__ __forceinline__ void split_df(double d, float& h, float& l, int& bad) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-    const unsigned hi = unsigned(u >> 32), lo = unsigned(u);
-    const unsigned sg = hi & 0x80000000u;
-    const int e = int((hi >> 20) & 0x7FFu);
-    const int E = e - 1023;
-    const bool zero = e == 0;   // zero or subnormal (below 1e-307): taken as zero
-    bad |= (!zero && (E < -100 || E > 127)) ? 1 : 0;
-    const int Ec = min(max(E, -100), 127);
-    const unsigned mtop = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const unsigned b = sg | (unsigned(Ec + 104) << 23);   // 2^(E-23), sign of d
-    const float hv = __uint_as_float(sg | (unsigned(Ec + 127) << 23) | mtop);
-    const float lv = __fsub_rn(__uint_as_float(b | ((lo & 0x1FFFFFFFu) >> 6)), __uint_as_float(b));
-    h = zero ? 0.f : hv;
-    l = zero ? 0.f : lv;
-}
-
-// (s, t) += a b, a = a1 + a2, b = b1 + b2
-__device__ __forceinline__ void df_mac(float& s, float& t, float a1, float a2, float b1, float b2) {
-    const float p = __fmul_rn(a1, b1);
-    float e = __fmaf_rn(a1, b1, -p);
-    e = __fmaf_rn(a1, b2, e);
-    e = __fmaf_rn(a2, b1, e);
-    const float sn = __fadd_rn(s, p);
-    const float v = __fsub_rn(sn, s);
-    t = __fadd_rn(t, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(sn, v)), __fsub_rn(p, v)), e));
-    s = sn;
-}
-
-__device__ __forceinline__ void df_renorm(float& s, float& t) {
-    const float sn = __fadd_rn(s, t);
-    t = __fsub_rn(t, __fsub_rn(sn, s));
-    s = sn;
-}
-
+// (split_df, df_mac and df_renorm are in common.cuh.)
 // NC right-hand sides per pass (1, 2, 4 or 8: register use grows with NC);
 // 8 entries of Z are loaded ahead of their use.
 template <int NC>
