@@ -362,6 +362,7 @@ static int solve_transposed(frico_gpu_ctx* ctx, const std::vector<cd>& B, int nr
         return rc;
     const dim3 tg((n + 31) / 32, (n + 31) / 32), tb(32, 8);
     if (mixed) {
+        if ((rc = trsv_dinv64_fp32(ctx))) return rc;
         k_transpose<float2><<<tg, tb, 0, st>>>((const float2*)ctx->z32.p, n, n, (float2*)ctx->lut.p, n);
         k_transpose_dinv<float2><<<2 * nb, 256, 0, st>>>((const float2*)ctx->dinv.p, nb, (float2*)ctx->dinv_t.p);
     } else {

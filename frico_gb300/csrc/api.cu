@@ -415,7 +415,12 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
             rc = refine_solve(ctx);
         }
         if (rc == FRICO_GPU_ENOCONV && piv == FRICO_PIVOT_AUTO) {
-            // complex64 factors cannot refine this system: FP64 LU of the resident Z
+            // complex64 factors cannot refine this system: FP64 LU of Z, assembled again in
+            // FP64 arithmetic if the resident one came from the double-float kernels
+            if (ctx->z_df) {
+                StageTimer tf(ctx, &ctx->stats.fill_ms);
+                if ((rc = fill_matrix(ctx, ctx->freq, true))) return rc;
+            }
             StageTimer tm(ctx, &ctx->stats.factor_ms);
             rc = lu_factor_fp64(ctx);
             if (rc) return rc;

@@ -181,6 +181,7 @@ struct frico_gpu_ctx {
     // fill
     double freq = 0.0;
     bool z_valid = false;         // Z64 holds the matrix of `freq`
+    bool z_df = false;            // ... assembled in double-float (mixed precision only)
     frico::DevBuf gtab, smom, basis_aux, z64, z32;
 
     // factorisation / solve
@@ -195,6 +196,7 @@ struct frico_gpu_ctx {
     frico::DevBuf dinv128;           // no-pivot complex64 LU: 128 x 128 blocks L^-1, U^-1, then the chain M blocks
     frico::DevBuf trsv_x;            // intermediate of the 128-row chained solves
     bool dinv128_valid = false;      // dinv128 belongs to the current complex64 factors
+    bool dinv64_stale = false;       // dinv (64-row blocks) not yet computed for them
     int trsv_epoch = 0;
     bool solved = false;
 
@@ -248,7 +250,7 @@ inline void count_launch(frico_gpu_ctx* ctx, int64_t k = 1) { ctx->stats.kernel_
 
 // ---- kernels' host launchers (defined in the .cu files) ----
 int build_quadrature(frico_gpu_ctx* ctx);                     // fill.cu
-int fill_matrix(frico_gpu_ctx* ctx, double freq);             // fill.cu
+int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only = false);   // fill.cu
 int symmetrize(frico_gpu_ctx* ctx);                           // fill.cu
 int lu_factor_fp64(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_factor_fp32(frico_gpu_ctx* ctx);                       // lu.cu
@@ -256,6 +258,8 @@ int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb);   // l
 int refine_solve(frico_gpu_ctx* ctx);                         // lu.cu
 int trsv_prepare_fp64(frico_gpu_ctx* ctx);                    // trsv.cu
 int trsv_prepare_fp32(frico_gpu_ctx* ctx);                    // trsv.cu
+int trsv_prepare_nopiv(frico_gpu_ctx* ctx);                   // trsv.cu
+int trsv_dinv64_fp32(frico_gpu_ctx* ctx);                     // trsv.cu
 int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw);  // trsv.cu
 int trsv_solve_fp32(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw);   // trsv.cu
 int trsv_check(frico_gpu_ctx* ctx, DeviceStatus* out = nullptr);   // trsv.cu

@@ -566,18 +566,19 @@ __global__ void __launch_bounds__(256) k_assemble_sym0(AsmArgs A) {
     const int64_t j = int64_t(J) * 32 + jl;
     const bool jok = j < A.n;
     BasisDF dj;
-    if (jok) dj = A.bdf[j];
+    const BasisDF* bdf = A.bdf ? A.bdf : nullptr;
+    if (jok) dj = bdf ? bdf[j] : BasisDF{A.bas[j].itm, A.bas[j].itp};
 #pragma unroll 1
     for (int kk = 0; kk < 4; kk++) {
         const int il = il0 + 8 * kk;
         const int64_t i = int64_t(I) * 32 + il;
         if (jok && i < A.n) {
-            const BasisDF di = A.bdf[i];
+            const BasisDF di = bdf ? bdf[i] : BasisDF{A.bas[i].itm, A.bas[i].itp};
             const bool shared = dj.itm == di.itm || dj.itm == di.itp || dj.itp == di.itm || dj.itp == di.itp;
             double2 e;
             float2 e32;
             float2 er, ei;
-            if (!shared && !(di.bad | dj.bad) && entry_mode0_df(A, di, dj, er, ei)) {
+            if (A.bdf && !shared && !(di.bad | dj.bad) && entry_mode0_df(A, di, dj, er, ei)) {
                 e = make_double2(f2d_exact(er.x) + f2d_exact(er.y), f2d_exact(ei.x) + f2d_exact(ei.y));
                 e32 = make_float2(__fadd_rn(er.x, er.y), __fadd_rn(ei.x, ei.y));
             } else {
@@ -665,7 +666,7 @@ static RwgDev rwg_dev(frico_gpu_ctx* ctx) {
     return r;
 }
 
-int fill_matrix(frico_gpu_ctx* ctx, double freq) {
+int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only) {
     int rc;
     if (ctx->geo_degree != ctx->opt.degree)
         if ((rc = build_quadrature(ctx))) return rc;
@@ -713,7 +714,11 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq) {
     a.ldz = n;
     a.inv_ksq = inv_ksq;
     a.bas = (const BasisAsm*)ctx->basis_aux.p;
-    a.bdf = bdf;
+    // double-float entries for the mixed path only: the FP64 drop-in (and the FP64
+    // factorisation a mixed solve falls back to) keep FP64 arithmetic throughout
+    const bool df = mode == 0 && ctx->opt.precision == FRICO_PREC_MIXED && !fp64_only;
+    a.bdf = df ? bdf : nullptr;
+    ctx->z_df = df;
     a.G = G;
     a.S = (const double2*)ctx->smom.p;
     a.Z64 = (double2*)ctx->z64.p;

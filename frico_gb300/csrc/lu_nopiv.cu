@@ -569,8 +569,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     if (hs.info != 0) return FRICO_GPU_OK;
     if ((rc = cuda_check(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(DeviceStatus), st), "status reset")))
         return rc;
-    if ((rc = trsv_prepare_fp32(ctx))) return rc;   // 64-row blocks too (transposed solves of the adjoint)
-    ctx->dinv128_valid = true;
+    if ((rc = trsv_prepare_nopiv(ctx))) return rc;
     return FRICO_GPU_OK;
 }
 

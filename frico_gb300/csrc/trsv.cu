@@ -220,44 +220,46 @@ __device__ __forceinline__ void st_relaxed_f2(float2* p, float2 v) {
 }
 
 // M_b for the chained solves: blockIdx.y = 0: Linv_b L_{b,b-1} (b >= 1), 1: Uinv_b U_{b,b+1}
-// (b <= nb - 2); 128 x 128 column-major into M + (y nb + b) 128^2. Operands go
-// through shared memory in 16-wide slabs; thread (tx, ty) owns rows ty + 16 i,
-// columns tx + 16 j.
+// (b <= nb - 2); 128 x 128 column-major into M + (y nb + b) 128^2. blockIdx.z picks
+// the 64 x 64 quadrant of the product; operands go through shared memory in 16-wide
+// slabs; thread (tx, ty) owns rows ty + 16 i, columns tx + 16 j (i, j < 4).
 __global__ void __launch_bounds__(256) k_chain_mats(const float2* __restrict__ LU, int64_t lda, int n,
                                                     const float2* __restrict__ Dinv, float2* __restrict__ M) {
-    __shared__ float2 As[kB2][17];       // As[r][k]
-    __shared__ float2 Bs[16][kB2 + 1];   // Bs[k][j]
+    __shared__ float2 As[64][17];       // As[r][k]
+    __shared__ float2 Bs[16][64 + 1];   // Bs[k][j]
     const int nb = (n + kB2 - 1) / kB2, b = blockIdx.x, upper = blockIdx.y;
     if (upper ? b >= nb - 1 : b == 0) return;
+    const int qr = (blockIdx.z & 1) * 64, qc = (blockIdx.z >> 1) * 64;
     const float2* D = Dinv + (size_t(upper) * nb + b) * kB2 * kB2;
     const int r0 = b * kB2, bs = min(kB2, n - r0);
     const int cb = upper ? b + 1 : b - 1, c0 = cb * kB2, cs = min(kB2, n - c0);
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    float2 acc[8][8];
+    float2 acc[4][4];
 #pragma unroll
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int j = 0; j < 8; j++) acc[i][j] = make_float2(0.f, 0.f);
+        for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
     for (int k0 = 0; k0 < kB2; k0 += 16) {
         __syncthreads();
-        for (int idx = threadIdx.x; idx < kB2 * 16; idx += 256) {
-            const int r = idx & (kB2 - 1), k = idx >> 7;
-            As[r][k] = D[int64_t(k0 + k) * kB2 + r];
-            const int kk = idx & 15, j = idx >> 4;   // T block row k0 + kk (of block b), column j (of block cb)
-            Bs[kk][j] = (k0 + kk < bs && j < cs) ? LU[int64_t(c0 + j) * lda + r0 + k0 + kk] : make_float2(0.f, 0.f);
+        for (int idx = threadIdx.x; idx < 64 * 16; idx += 256) {
+            const int r = idx & 63, k = idx >> 6;
+            As[r][k] = D[int64_t(k0 + k) * kB2 + qr + r];
+            const int kk = idx & 15, j = idx >> 4;   // T block row k0 + kk (of block b), column qc + j (of block cb)
+            Bs[kk][j] = (k0 + kk < bs && qc + j < cs) ? LU[int64_t(c0 + qc + j) * lda + r0 + k0 + kk]
+                                                      : make_float2(0.f, 0.f);
         }
         __syncthreads();
 #pragma unroll 4
         for (int k = 0; k < 16; k++) {
-            float2 a[8], bv[8];
+            float2 a[4], bv[4];
 #pragma unroll
-            for (int i = 0; i < 8; i++) a[i] = As[ty + 16 * i][k];
+            for (int i = 0; i < 4; i++) a[i] = As[ty + 16 * i][k];
 #pragma unroll
-            for (int j = 0; j < 8; j++) bv[j] = Bs[k][tx + 16 * j];
+            for (int j = 0; j < 4; j++) bv[j] = Bs[k][tx + 16 * j];
 #pragma unroll
-            for (int i = 0; i < 8; i++)
+            for (int i = 0; i < 4; i++)
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
+                for (int j = 0; j < 4; j++) {
                     acc[i][j].x = fmaf(a[i].x, bv[j].x, fmaf(-a[i].y, bv[j].y, acc[i][j].x));
                     acc[i][j].y = fmaf(a[i].x, bv[j].y, fmaf(a[i].y, bv[j].x, acc[i][j].y));
                 }
@@ -265,9 +267,9 @@ __global__ void __launch_bounds__(256) k_chain_mats(const float2* __restrict__ L
     }
     float2* out = M + (size_t(upper) * nb + b) * kB2 * kB2;
 #pragma unroll
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int j = 0; j < 8; j++) out[(tx + 16 * j) * kB2 + ty + 16 * i] = acc[i][j];
+        for (int j = 0; j < 4; j++) out[(qc + tx + 16 * j) * kB2 + qr + ty + 16 * i] = acc[i][j];
 }
 
 // NC: right-hand sides per launch (1, 2, 4 or 8), a compile-time bound on the column loops
@@ -450,6 +452,7 @@ int trsv_prepare(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_b
     const int n = int(ctx->n), nb = (n + kB - 1) / kB;
     int rc;
     ctx->dinv128_valid = false;   // set again by the no-pivot factorisation, which fills dinv128
+    ctx->dinv64_stale = false;
     if ((rc = ensure(ctx, ws_buf, sizeof(C) * size_t(2) * nb * kB * kB))) return rc;
     if ((rc = ensure(ctx, flag_buf, sizeof(int) * (nb + 64)))) return rc;
     if ((rc = cuda_check(ctx, cudaMemsetAsync(flag_buf.p, 0, sizeof(int) * (nb + 64), ctx->stream), "flags")))
@@ -486,6 +489,32 @@ int trsv_solve(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_buf
 int trsv_prepare_fp64(frico_gpu_ctx* ctx) {
     return trsv_prepare<double2>(ctx, (const double2*)ctx->z64.p, ctx->dinv, ctx->trsv_flags);
 }
+// After the no-pivot factorisation: the chain flags and ticket (the 128-row solves
+// use the ticket); the 64-row inverted blocks are left for first use
+// (trsv_dinv64_fp32), they only serve the transposed solves of the adjoint.
+int trsv_prepare_nopiv(frico_gpu_ctx* ctx) {
+    const int nb = int((ctx->n + kB - 1) / kB);
+    int rc;
+    if ((rc = ensure(ctx, ctx->trsv_flags, sizeof(int) * (nb + 64)))) return rc;
+    if ((rc = cuda_check(ctx, cudaMemsetAsync(ctx->trsv_flags.p, 0, sizeof(int) * (nb + 64), ctx->stream), "flags")))
+        return rc;
+    ctx->dinv64_stale = true;
+    ctx->dinv128_valid = true;
+    return FRICO_GPU_OK;
+}
+
+int trsv_dinv64_fp32(frico_gpu_ctx* ctx) {
+    if (!ctx->dinv64_stale) return FRICO_GPU_OK;
+    const int n = int(ctx->n), nb = (n + kB - 1) / kB;
+    int rc;
+    if ((rc = ensure(ctx, ctx->dinv, sizeof(float2) * size_t(2) * nb * kB * kB))) return rc;
+    float2* Linv = (float2*)ctx->dinv.p;
+    k_invert_diag<float2><<<nb, 128, 0, ctx->stream>>>((const float2*)ctx->z32.p, n, n, Linv, Linv + size_t(nb) * kB * kB);
+    count_launch(ctx);
+    ctx->dinv64_stale = false;
+    return cuda_check(ctx, cudaGetLastError(), "k_invert_diag");
+}
+
 int trsv_prepare_fp32(frico_gpu_ctx* ctx) {
     return trsv_prepare<float2>(ctx, (const float2*)ctx->z32.p, ctx->dinv, ctx->trsv_flags);
 }
@@ -496,7 +525,7 @@ int trsv_solve_fp64(frico_gpu_ctx* ctx, double2* W, int nrhs, int64_t ldw) {
 int trsv128_prepare(frico_gpu_ctx* ctx, cudaStream_t st) {
     const int n = int(ctx->n), nb = (n + kB2 - 1) / kB2;
     const float2* Dinv = (const float2*)ctx->dinv128.p;
-    k_chain_mats<<<dim3(nb, 2), 256, 0, st>>>((const float2*)ctx->z32.p, n, n, Dinv,
+    k_chain_mats<<<dim3(nb, 2, 4), 256, 0, st>>>((const float2*)ctx->z32.p, n, n, Dinv,
                                               (float2*)ctx->dinv128.p + size_t(2) * nb * kB2 * kB2);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_chain_mats");
