@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "dunavant_rules.h"
 
 namespace frico {
@@ -312,6 +313,69 @@ __global__ void __launch_bounds__(256) k_gtab_sym(int64_t nt, const QPoint* __re
     }
 }
 
+// k_gtab_sym<0> in double-float for the mixed path: g = exp(-jkR)/R with R from
+// the FP64 coordinate differences (r^2 in FP64, then split), sqrt, 1/R and
+// sincos(kR) in double-float (dfloat.cuh); stored as (re hi, re lo, im hi,
+// im lo). A pair outside the double-float range (kR >= 6400, r^2 beyond the
+// split's exponents) is evaluated in FP64 and then split.
+__global__ void __launch_bounds__(256) k_gtab_sym_df(int64_t nt, const QPoint* __restrict__ qp, double k,
+                                                    float4* __restrict__ G) {
+    __shared__ double pa[32][3], pb[32][3];
+    __shared__ float4 tile[32][33];
+    const int64_t T = (nt + 31) / 32;
+    int64_t lin = blockIdx.x, ta = 0;
+    while (lin >= T - ta) { lin -= T - ta; ta++; }
+    const int64_t tb = ta + lin;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    if (threadIdx.x < 64) {
+        int which = threadIdx.x >> 5, q = threadIdx.x & 31;
+        int64_t t = (which ? tb : ta) * 32 + q;
+        double* dst = which ? pb[q] : pa[q];
+        if (t < nt) {
+            QPoint p = qp[t];
+            dst[0] = p.x; dst[1] = p.y; dst[2] = p.z;
+        } else {
+            dst[0] = dst[1] = dst[2] = 0.0;
+        }
+    }
+    __syncthreads();
+    int kbad = 0;
+    const dfl kd = df_from_double(k, kbad);
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t a = ta * 32 + r, b = tb * 32 + tx;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (a < nt && b < nt) {
+            if (a != b) {
+                const double dx = pa[r][0] - pb[tx][0], dy = pa[r][1] - pb[tx][1], dz = pa[r][2] - pb[tx][2];
+                const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+                int bad = kbad;
+                const dfl R = df_sqrt(df_from_double(r2, bad));
+                dfl s, c;
+                if (!bad && df_sincos(df_mul(kd, R), s, c)) {
+                    const dfl inv = df_rcp(R);
+                    const dfl gr = df_mul(c, inv), gi = df_neg(df_mul(s, inv));
+                    g = make_float4(gr.h, gr.l, gi.h, gi.l);
+                } else {
+                    const double Rd = sqrt(r2);
+                    double sd, cd;
+                    sincos(k * Rd, &sd, &cd);
+                    int b2 = 0;
+                    const dfl gr = df_from_double(cd / Rd, b2), gi = df_from_double(-sd / Rd, b2);
+                    g = make_float4(gr.h, gr.l, gi.h, gi.l);
+                }
+            }
+            G[a * nt + b] = g;
+        }
+        tile[r][tx] = g;
+    }
+    if (ta == tb) return;
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t a = tb * 32 + r, b = ta * 32 + tx;   // transposed tile
+        if (a < nt && b < nt) G[a * nt + b] = tile[tx][r];
+    }
+}
+
 // Moments of g over point sets P (test, about ca) and Q (source, about cb):
 // m[0] = sum w w g, m[1..3] = sum w w g (p-ca), m[4..6] = sum w w g (q-cb),
 // m[7] = sum w w g (p-ca).(q-cb).
@@ -382,6 +446,7 @@ struct AsmArgs {
     const BasisAsm* bas;
     const BasisDF* bdf;  // the same, double-float (mode 0)
     const double2* G;    // mode 0/2: [nt*nt]; mode 1: 8 planes
+    const float4* G4;    // mode 0, mixed: the table in double-float (re hi, re lo, im hi, im lo), else null
     const double2* S;    // split moments [n*4*8]
     double2* Z64;        // may be null
     float2* Z32;         // may be null
@@ -500,7 +565,13 @@ __device__ __forceinline__ double2 entry_mode0(const AsmArgs& A, const BasisAsm&
             const double* uj = t ? bj.u_p : bj.u_m;
             const double f = fma(ui[0], uj[0], fma(ui[1], uj[1], fma(ui[2], uj[2], (s ? bi.hk_p : bi.hk_m) *
                                                                                    (t ? bj.hs_p : bj.hs_m))));
-            const double2 g = A.G[int64_t(ta) * A.nt + tb];
+            double2 g;
+            if (A.G4) {
+                const float4 q = A.G4[int64_t(ta) * A.nt + tb];
+                g = make_double2(df_to_double(dmk(q.x, q.y)), df_to_double(dmk(q.z, q.w)));
+            } else {
+                g = A.G[int64_t(ta) * A.nt + tb];
+            }
             entry.x = fma(g.x, f, entry.x);
             entry.y = fma(g.y, f, entry.y);
         }
@@ -510,9 +581,8 @@ __device__ __forceinline__ double2 entry_mode0(const AsmArgs& A, const BasisAsm&
 
 // One mode-0 entry in double-float for RWGs that share no triangle (all four
 // blocks are table blocks): sum over the blocks of g_ab f_ab with
-// f_ab = u_ia . u_jb + hk_ia hs_jb, the same terms as entry_mode0. Returns
-// false when a table value is outside the split's range (the caller then takes
-// the FP64 path); (er, ei) = the entry as (hi, lo) pairs.
+// f_ab = u_ia . u_jb + hk_ia hs_jb, the same terms as entry_mode0, from the
+// double-float table; (er, ei) = the entry as (hi, lo) pairs.
 __device__ __forceinline__ bool entry_mode0_df(const AsmArgs& A, const BasisDF& di, const BasisDF& dj, float2& er,
                                                float2& ei) {
     float rs = 0.f, rt = 0.f, is = 0.f, it = 0.f;
@@ -532,12 +602,9 @@ __device__ __forceinline__ bool entry_mode0_df(const AsmArgs& A, const BasisDF& 
         df_mac(fs, ft, ui[2][0], ui[2][1], uj[2][0], uj[2][1]);
         df_mac(fs, ft, hk[0], hk[1], hs[0], hs[1]);
         df_renorm(fs, ft);
-        const double2 g = A.G[int64_t(ta) * A.nt + tb];
-        float gx1, gx2, gy1, gy2;
-        split_df(g.x, gx1, gx2, bad);
-        split_df(g.y, gy1, gy2, bad);
-        df_mac(rs, rt, gx1, gx2, fs, ft);
-        df_mac(is, it, gy1, gy2, fs, ft);
+        const float4 g = A.G4[int64_t(ta) * A.nt + tb];
+        df_mac(rs, rt, g.x, g.y, fs, ft);
+        df_mac(is, it, g.z, g.w, fs, ft);
     }
     df_renorm(rs, rt);
     df_renorm(is, it);
@@ -698,7 +765,12 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only) {
     double2* G = (double2*)ctx->gtab.p;
     const int64_t T = (nt + 31) / 32;
     const unsigned sym_blocks = unsigned(T * (T + 1) / 2);
-    if (mode == 0) {
+    // double-float table and entries for the mixed path only: the FP64 drop-in (and the FP64
+    // factorisation a mixed solve falls back to) keep FP64 arithmetic throughout
+    const bool df = mode == 0 && ctx->opt.precision == FRICO_PREC_MIXED && !fp64_only;
+    if (df) {
+        k_gtab_sym_df<<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, k, (float4*)G);
+    } else if (mode == 0) {
         k_gtab_sym<0><<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, geo, k, G);
     } else if (mode == 1) {
         k_gtab_moments<<<gt, 128, 0, st>>>(nt, geo, qp, nq, k, G);
@@ -714,10 +786,8 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only) {
     a.ldz = n;
     a.inv_ksq = inv_ksq;
     a.bas = (const BasisAsm*)ctx->basis_aux.p;
-    // double-float entries for the mixed path only: the FP64 drop-in (and the FP64
-    // factorisation a mixed solve falls back to) keep FP64 arithmetic throughout
-    const bool df = mode == 0 && ctx->opt.precision == FRICO_PREC_MIXED && !fp64_only;
     a.bdf = df ? bdf : nullptr;
+    a.G4 = df ? (const float4*)G : nullptr;
     ctx->z_df = df;
     a.G = G;
     a.S = (const double2*)ctx->smom.p;

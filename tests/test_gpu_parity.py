@@ -185,6 +185,19 @@ def test_mixed_singular_falls_back_then_reports(gpu_lib):
     assert sim.stats()["pivoting_used"] == 1
 
 
+@pytest.mark.parametrize("mesh,f", [("sphere3", 450e6), ("bowtie1500", 250e6), ("bowtie1500", 800e6)])
+def test_double_float_fill_matches_fp64(gpu_lib, mesh, f):
+    """The mixed path fills Z64 with the double-float Green table and assembly
+    (FP32 pipe); the FP64 drop-in with FP64 arithmetic. Entrywise the two agree
+    to 2e-13 of max |Z| (and the FP64 one stays the oracle-parity fill)."""
+    m = meshes.icosphere(3) if mesh == "sphere3" else meshes.bowtie_preset(1500)
+    Zd = Simulation(m, precision="mixed").compute_matrix(f, download=True)
+    Z6 = Simulation(m, precision="fp64").compute_matrix(f, download=True)
+    err = np.abs(Zd - Z6).max() / np.abs(Z6).max()
+    assert err < 2e-13, err
+    assert rel_entrywise(Zd, Z6, floor_frac=1e-6) < 1e-9
+
+
 @pytest.mark.parametrize("nrhs", [1, 3])
 def test_double_float_residual_matches_fp64(gpu_lib, nrhs):
     """The refinement residual in double-float (FP64 Z split into FP32 pairs on
