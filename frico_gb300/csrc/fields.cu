@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace frico {
 
@@ -120,6 +121,7 @@ static const int kFT = 128;   // triangles staged per shared-memory round
 
 // Partial E/H sums for a block of points over one chunk of triangles.
 // part[(chunk * npts + p) * 6 + {Ex,Ey,Ez,Hx,Hy,Hz}]
+template <bool WITH_H>
 __global__ void __launch_bounds__(kFP) k_fields_part(int64_t npts, const double* __restrict__ P, int64_t nt,
                                                     int64_t tri_per_chunk, const TriGeo* __restrict__ geo,
                                                     const double2* __restrict__ AJ,
@@ -135,6 +137,7 @@ __global__ void __launch_bounds__(kFP) k_fields_part(int64_t npts, const double*
     double2 E[3], H[3];
     for (int a = 0; a < 3; a++) E[a] = H[a] = make_double2(0, 0);
     const double2 mjwmu = make_double2(-0.0 * FRICO_MU0, -omega * FRICO_MU0);  // (-j omega) * MU0
+    const double invk2 = 1.0 / (k * k);
     for (int64_t tb = t0; tb < t1; tb += kFT) {
         const int cnt = int(min(int64_t(kFT), t1 - tb));
         __syncthreads();
@@ -151,33 +154,165 @@ __global__ void __launch_bounds__(kFP) k_fields_part(int64_t npts, const double*
             for (int q = 0; q < cnt; q++) {
                 const double vx = px - sb[q][0], vy = py - sb[q][1], vz = pz - sb[q][2];
                 const double R = sqrt(vx * vx + vy * vy + vz * vz);
-                const double _4piR = 4 * M_PI * R;
-                const double _4piR3 = _4piR * R * R;
+                // one division per pair: 1/(4 pi R), 1/(4 pi R^3) and 1/(kR)^2 from 1/R
+                const double invR = 1.0 / R;
+                const double inv4piR = invR * (0.25 * M_1_PI);
+                const double inv4piR3 = inv4piR * invR * invR;
                 const double kR = k * R;
                 double s, c;
                 sincos(kR, &s, &c);
-                const double2 g = make_double2(c / _4piR, -s / _4piR);
+                const double2 g = make_double2(c * inv4piR, -s * inv4piR);
                 const double2 J0 = sj[q][0], J1 = sj[q][1], J2 = sj[q][2];
                 const double2 t = cmul(sj[q][3], make_double2(1.0, kR));  // divJ*(1+jkR)
-                const double kR2 = kR * kR;
+                const double invkR2 = invR * invR * invk2;
                 const double vr[3] = {vx, vy, vz};
                 const double2 Jv[3] = {J0, J1, J2};
                 for (int a = 0; a < 3; a++) {
-                    double2 tv = cscale(t, vr[a]);
-                    double2 d = csub(Jv[a], make_double2(tv.x / kR2, tv.y / kR2));
+                    double2 tv = cscale(t, vr[a] * invkR2);
+                    double2 d = csub(Jv[a], tv);
                     E[a] = cadd(E[a], cmul(cmul(mjwmu, d), g));
                 }
-                // gradg = -((1+jkR)/_4piR3) * exp(+-jkR)
-                const double2 ph = hphase_physical ? make_double2(c, -s) : make_double2(c, s);
-                const double2 gg = cmul(make_double2(-(1.0 / _4piR3), -(kR / _4piR3)), ph);
-                const double2 rc[3] = {csub(cscale(J2, vy), cscale(J1, vz)), csub(cscale(J0, vz), cscale(J2, vx)),
-                                       csub(cscale(J1, vx), cscale(J0, vy))};
-                for (int a = 0; a < 3; a++) H[a] = cadd(H[a], cmul(rc[a], gg));
+                if (WITH_H) {
+                    // gradg = -((1+jkR)/_4piR3) * exp(+-jkR)
+                    const double2 ph = hphase_physical ? make_double2(c, -s) : make_double2(c, s);
+                    const double2 gg = cmul(make_double2(-inv4piR3, -kR * inv4piR3), ph);
+                    const double2 rc[3] = {csub(cscale(J2, vy), cscale(J1, vz)), csub(cscale(J0, vz), cscale(J2, vx)),
+                                           csub(cscale(J1, vx), cscale(J0, vy))};
+                    for (int a = 0; a < 3; a++) H[a] = cadd(H[a], cmul(rc[a], gg));
+                }
             }
     }
     if (p < npts) {
         double2* o = part + (blockIdx.y * npts + p) * 6;
         for (int a = 0; a < 3; a++) { o[a] = E[a]; o[3 + a] = H[a]; }
+    }
+}
+
+// The same partial sums in double-float for the mixed path (dfloat.cuh): the
+// point-centroid vector and R^2 from FP64 differences, then sqrt, 1/R,
+// sincos(kR) and every product and sum in double-float. With
+// G = exp(-jkR) / (4 pi R), w = 1/(kR)^2 + j/(kR) (that is (1 + jkR)/(kR)^2) and
+// U = divJ w G:  E_a += -j w mu (J_a G - v_a U),  H_a += (v x J)_a gg with
+// gg = -(1 + jkR) exp(+-jkR) / (4 pi R^3). Currents are split once per triangle
+// when staged. A pair outside the double-float range (kR >= 6400, R^2 beyond
+// the split's exponents) is summed in FP64.
+struct cdf {
+    dfl r, i;
+};
+__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
+    return cdf{df_add(df_mul(a.r, b.r), df_neg(df_mul(a.i, b.i))), df_add(df_mul(a.r, b.i), df_mul(a.i, b.r))};
+}
+__device__ __forceinline__ cdf cdf_scale(cdf a, dfl s) { return cdf{df_mul(a.r, s), df_mul(a.i, s)}; }
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return cdf{df_add(a.r, b.r), df_add(a.i, b.i)}; }
+__device__ __forceinline__ cdf cdf_sub(cdf a, cdf b) { return cdf{df_add(a.r, df_neg(b.r)), df_add(a.i, df_neg(b.i))}; }
+__device__ __forceinline__ cdf cdf_of(float4 q) { return cdf{dmk(q.x, q.y), dmk(q.z, q.w)}; }
+__device__ __forceinline__ float4 f4_of(double2 z, int& bad) {
+    float4 q;
+    split_df(z.x, q.x, q.y, bad);
+    split_df(z.y, q.z, q.w, bad);
+    return q;
+}
+
+template <bool WITH_H>
+__global__ void __launch_bounds__(kFP) k_fields_part_df(int64_t npts, const double* __restrict__ P, int64_t nt,
+                                                       int64_t tri_per_chunk, const TriGeo* __restrict__ geo,
+                                                       const double2* __restrict__ AJ,
+                                                       const double2* __restrict__ AdivJ, double k, double omega,
+                                                       int hphase_physical, double2* __restrict__ part) {
+    __shared__ double sb[kFT][3];
+    __shared__ float4 sj[kFT][4];      // J0, J1, J2, divJ as (re hi, re lo, im hi, im lo)
+    __shared__ double2 sjd[kFT][4];    // the same in FP64 (out-of-range pairs)
+    __shared__ int s_bad[kFT];
+    const int64_t p = blockIdx.x * int64_t(kFP) + threadIdx.x;
+    const int64_t t0 = blockIdx.y * tri_per_chunk;
+    const int64_t t1 = min(nt, t0 + tri_per_chunk);
+    double px = 0, py = 0, pz = 0;
+    if (p < npts) { px = P[3 * p]; py = P[3 * p + 1]; pz = P[3 * p + 2]; }
+    int kb = 0;
+    const dfl kd = df_from_double(k, kb), invk = df_from_double(1.0 / k, kb);
+    const dfl inv4pi = df_from_double(0.25 * M_1_PI, kb);
+    const dfl zero = dmk(0.f);
+    cdf E[3], H[3];
+    for (int a = 0; a < 3; a++) E[a] = H[a] = cdf{zero, zero};
+    double2 Ed[3], Hd[3];   // FP64 sums of out-of-range pairs
+    for (int a = 0; a < 3; a++) Ed[a] = Hd[a] = make_double2(0, 0);
+    for (int64_t tb = t0; tb < t1; tb += kFT) {
+        const int cnt = int(min(int64_t(kFT), t1 - tb));
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const double* c = geo[tb + q].c;
+            sb[q][0] = c[0]; sb[q][1] = c[1]; sb[q][2] = c[2];
+            int bad = 0;
+            for (int a = 0; a < 3; a++) {
+                sjd[q][a] = AJ[3 * (tb + q) + a];
+                sj[q][a] = f4_of(sjd[q][a], bad);
+            }
+            sjd[q][3] = AdivJ[tb + q];
+            sj[q][3] = f4_of(sjd[q][3], bad);
+            s_bad[q] = bad;
+        }
+        __syncthreads();
+        if (p < npts)
+            for (int q = 0; q < cnt; q++) {
+                const double vx = px - sb[q][0], vy = py - sb[q][1], vz = pz - sb[q][2];
+                const double r2 = fma(vx, vx, fma(vy, vy, vz * vz));
+                int bad = kb | s_bad[q];
+                const dfl v[3] = {df_from_double(vx, bad), df_from_double(vy, bad), df_from_double(vz, bad)};
+                const dfl R = df_sqrt(df_from_double(r2, bad));
+                dfl sn, cs;
+                if (!bad && df_sincos(df_mul(kd, R), sn, cs)) {
+                    const dfl invR = df_rcp(R);
+                    const dfl i4R = df_mul(invR, inv4pi);
+                    const cdf G{df_mul(cs, i4R), df_neg(df_mul(sn, i4R))};
+                    const dfl ikR = df_mul(invR, invk);
+                    const cdf w{df_mul(ikR, ikR), ikR};
+                    const cdf U = cdf_mul(cdf_of(sj[q][3]), cdf_mul(w, G));
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                        E[a] = cdf_add(E[a], cdf_sub(cdf_mul(cdf_of(sj[q][a]), G), cdf_scale(U, v[a])));
+                    if (WITH_H) {
+                        const dfl i4R3 = df_mul(i4R, df_mul(invR, invR));
+                        const dfl kR = df_mul(kd, R);
+                        const cdf ph{cs, hphase_physical ? df_neg(sn) : sn};
+                        // -(1 + jkR) ph / (4 pi R^3)
+                        const cdf gg = cdf_scale(cdf_mul(cdf{dmk(-1.f), df_neg(kR)}, ph), i4R3);
+                        const cdf J0 = cdf_of(sj[q][0]), J1 = cdf_of(sj[q][1]), J2 = cdf_of(sj[q][2]);
+                        const cdf rc[3] = {cdf_sub(cdf_scale(J2, v[1]), cdf_scale(J1, v[2])),
+                                           cdf_sub(cdf_scale(J0, v[2]), cdf_scale(J2, v[0])),
+                                           cdf_sub(cdf_scale(J1, v[0]), cdf_scale(J0, v[1]))};
+#pragma unroll
+                        for (int a = 0; a < 3; a++) H[a] = cdf_add(H[a], cdf_mul(rc[a], gg));
+                    }
+                } else {
+                    // FP64, as k_fields_part (without the -j w mu factor, applied at the end)
+                    const double R64 = sqrt(r2), invR = 1.0 / R64, i4R = invR * (0.25 * M_1_PI), kR = k * R64;
+                    double s, c;
+                    sincos(kR, &s, &c);
+                    const double2 g = make_double2(c * i4R, -s * i4R);
+                    const double2 t = cmul(sjd[q][3], make_double2(1.0, kR));
+                    const double ikR2 = invR * invR / (k * k);
+                    const double vr[3] = {vx, vy, vz};
+                    for (int a = 0; a < 3; a++) Ed[a] = cadd(Ed[a], cmul(csub(sjd[q][a], cscale(t, vr[a] * ikR2)), g));
+                    if (WITH_H) {
+                        const double i4R3 = i4R * invR * invR;
+                        const double2 ph = hphase_physical ? make_double2(c, -s) : make_double2(c, s);
+                        const double2 gg = cmul(make_double2(-i4R3, -kR * i4R3), ph);
+                        const double2 J0 = sjd[q][0], J1 = sjd[q][1], J2 = sjd[q][2];
+                        const double2 rc[3] = {csub(cscale(J2, vy), cscale(J1, vz)), csub(cscale(J0, vz), cscale(J2, vx)),
+                                               csub(cscale(J1, vx), cscale(J0, vy))};
+                        for (int a = 0; a < 3; a++) Hd[a] = cadd(Hd[a], cmul(rc[a], gg));
+                    }
+                }
+            }
+    }
+    if (p < npts) {
+        const double2 mjwmu = make_double2(-0.0 * FRICO_MU0, -omega * FRICO_MU0);  // (-j omega) * MU0
+        double2* o = part + (blockIdx.y * npts + p) * 6;
+        for (int a = 0; a < 3; a++) {
+            const double2 e = cadd(make_double2(df_to_double(E[a].r), df_to_double(E[a].i)), Ed[a]);
+            o[a] = cmul(mjwmu, e);
+            o[3 + a] = cadd(make_double2(df_to_double(H[a].r), df_to_double(H[a].i)), Hd[a]);
+        }
     }
 }
 
@@ -270,6 +405,25 @@ int lump_currents(frico_gpu_ctx* ctx, int col) {
     return FRICO_GPU_OK;
 }
 
+// Partial-sum kernel for the context's precision: double-float for the mixed path
+// (its results are checked against the FP64 path to 1e-12), FP64 for the drop-in.
+static void launch_fields_part(frico_gpu_ctx* ctx, dim3 grid, cudaStream_t st, bool with_h, int64_t npts,
+                               const double* P, int64_t nt, int64_t tpc, double k, double omega, double2* part) {
+    const TriGeo* geo = (const TriGeo*)ctx->trigeo.p;
+    const double2* aj = (const double2*)ctx->tri_aj.p;
+    const double2* adj = (const double2*)ctx->tri_adivj.p;
+    const int hp = ctx->opt.h_phase_mode == FRICO_HPHASE_PHYSICAL;
+    const bool df = ctx->opt.precision == FRICO_PREC_MIXED;
+    if (df && with_h)
+        k_fields_part_df<true><<<grid, kFP, 0, st>>>(npts, P, nt, tpc, geo, aj, adj, k, omega, hp, part);
+    else if (df)
+        k_fields_part_df<false><<<grid, kFP, 0, st>>>(npts, P, nt, tpc, geo, aj, adj, k, omega, hp, part);
+    else if (with_h)
+        k_fields_part<true><<<grid, kFP, 0, st>>>(npts, P, nt, tpc, geo, aj, adj, k, omega, hp, part);
+    else
+        k_fields_part<false><<<grid, kFP, 0, st>>>(npts, P, nt, tpc, geo, aj, adj, k, omega, hp, part);
+}
+
 int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_host, double2* E_host,
                     double2* H_host) {
     int rc;
@@ -294,10 +448,8 @@ int eval_fields_dev(frico_gpu_ctx* ctx, int col, int64_t npts, const double* P_h
     if ((rc = cuda_check(ctx, cudaMemcpyAsync(pts.p, P_host, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice,
                                               ctx->stream), "points")))
         return rc;
-    k_fields_part<<<dim3(unsigned(pblocks), unsigned(nchunks)), kFP, 0, ctx->stream>>>(
-        npts, (const double*)pts.p, nt, tpc, (const TriGeo*)ctx->trigeo.p, (const double2*)ctx->tri_aj.p,
-        (const double2*)ctx->tri_adivj.p, k, omega, ctx->opt.h_phase_mode == FRICO_HPHASE_PHYSICAL,
-        (double2*)ctx->fld_part.p);
+    launch_fields_part(ctx, dim3(unsigned(pblocks), unsigned(nchunks)), ctx->stream, H_host != nullptr, npts,
+                       (const double*)pts.p, nt, tpc, k, omega, (double2*)ctx->fld_part.p);
     k_fields_reduce<<<unsigned((npts * 6 + 255) / 256), 256, 0, ctx->stream>>>(
         npts, int(nchunks), (const double2*)ctx->fld_part.p, (double2*)ctx->fld_out.p);
     count_launch(ctx, 2);
@@ -394,9 +546,8 @@ int eval_fields_noalloc(frico_gpu_ctx* ctx, int col, int64_t npts, const double*
     nchunks = std::min<int64_t>(nchunks, kNoAllocScratch / (6 * npts));
     const int64_t tpc = (nt + nchunks - 1) / nchunks;
     nchunks = (nt + tpc - 1) / tpc;
-    k_fields_part<<<dim3(unsigned(pblocks), unsigned(nchunks)), kFP, 0, ctx->stream>>>(
-        npts, P_dev, nt, tpc, (const TriGeo*)ctx->trigeo.p, (const double2*)ctx->tri_aj.p,
-        (const double2*)ctx->tri_adivj.p, k, omega, ctx->opt.h_phase_mode == FRICO_HPHASE_PHYSICAL, part);
+    launch_fields_part(ctx, dim3(unsigned(pblocks), unsigned(nchunks)), ctx->stream, H_dev != nullptr, npts, P_dev, nt,
+                       tpc, k, omega, part);
     k_fields_reduce_split<<<unsigned((npts * 6 + 255) / 256), 256, 0, ctx->stream>>>(npts, int(nchunks), part, E_dev,
                                                                                      H_dev);
     count_launch(ctx, 2);

@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(kMP) k_fields_multi(int64_t npts, const double
 #pragma unroll
         for (int a = 0; a < 3; a++) E[r][a] = H[r][a] = make_double2(0, 0);
     const double2 mjwmu = make_double2(-0.0 * FRICO_MU0, -omega * FRICO_MU0);
+    const double invk2 = 1.0 / (k * k);
     for (int64_t tb = t0; tb < t1; tb += kMT) {
         const int cnt = int(min(int64_t(kMT), t1 - tb));
         __syncthreads();
@@ -72,24 +73,25 @@ __global__ void __launch_bounds__(kMP) k_fields_multi(int64_t npts, const double
             for (int q = 0; q < cnt; q++) {
                 const double vx = px - sc[q][0], vy = py - sc[q][1], vz = pz - sc[q][2];
                 const double R = sqrt(vx * vx + vy * vy + vz * vz);
-                const double _4piR = 4 * M_PI * R;
+                // one division per pair: 1/(4 pi R), 1/(4 pi R^3) and 1/(kR)^2 from 1/R
+                const double invR = 1.0 / R;
+                const double inv4piR = invR * (0.25 * M_1_PI);
                 const double kR = k * R;
                 double s, c;
                 sincos(kR, &s, &c);
-                const double2 g = make_double2(c / _4piR, -s / _4piR);
+                const double2 g = make_double2(c * inv4piR, -s * inv4piR);
                 const double2 c1 = cmul(mjwmu, g);
-                const double kR2 = kR * kR;
                 // -c1 (1 + jkR) / kR^2
-                const double2 m = cscale(cmul(c1, make_double2(1.0, kR)), -1.0 / kR2);
+                const double2 m = cscale(cmul(c1, make_double2(1.0, kR)), -(invR * invR * invk2));
                 const double vr[3] = {vx, vy, vz};
                 double2 c2[3];
 #pragma unroll
                 for (int a = 0; a < 3; a++) c2[a] = cscale(m, vr[a]);
                 double2 gv[3];
                 if (WITH_H) {
-                    const double _4piR3 = _4piR * R * R;
+                    const double inv4piR3 = inv4piR * invR * invR;
                     const double2 ph = hphase_physical ? make_double2(c, -s) : make_double2(c, s);
-                    const double2 gg = cmul(make_double2(-(1.0 / _4piR3), -(kR / _4piR3)), ph);
+                    const double2 gg = cmul(make_double2(-inv4piR3, -kR * inv4piR3), ph);
 #pragma unroll
                     for (int a = 0; a < 3; a++) gv[a] = cscale(gg, vr[a]);
                 }

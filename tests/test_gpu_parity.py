@@ -198,6 +198,30 @@ def test_double_float_fill_matches_fp64(gpu_lib, mesh, f):
     assert rel_entrywise(Zd, Z6, floor_frac=1e-6) < 1e-9
 
 
+def test_double_float_fields_match_fp64(gpu_lib):
+    """The mixed path evaluates fields in double-float (E, and H when asked
+    for); the FP64 drop-in in FP64. On the same scatterer their E and H agree to
+    1e-9 (the two solutions differ by about 1e-11), far and near."""
+    m = meshes.icosphere(3)
+    f = 450e6
+    _, _, far = meshes.bistatic_cuts(10.0)
+    rng = np.random.default_rng(7)
+    d = rng.standard_normal((64, 3))
+    near = d / np.linalg.norm(d, axis=1)[:, None] * rng.uniform(1.3, 3.0, (64, 1))
+    out = {}
+    for prec in ("mixed", "fp64"):
+        sim = Simulation(m, precision=prec)
+        sim.compute_matrix(f)
+        sim.set_nrhs(1)
+        sim.update_rhs(f, PlaneWave(0.4, 1.1, 1.0, 0.5))
+        sim.solve()
+        Ef, _ = sim.eval_fields(far)
+        En, Hn = sim.eval_fields(near)
+        out[prec] = (Ef, En, Hn, sim.bistatic_rcs(10.0))
+    for a, b in zip(out["mixed"], out["fp64"]):
+        assert rel_norm(a, b) < 1e-9
+
+
 @pytest.mark.parametrize("nrhs", [1, 3])
 def test_double_float_residual_matches_fp64(gpu_lib, nrhs):
     """The refinement residual in double-float (FP64 Z split into FP32 pairs on

@@ -67,8 +67,10 @@ def test_fields_multi_match_single_column(gpu_lib):
     sig = sim.rcs_points_multi(10.0, th, ph)
     assert E.shape == (ncols, 37, 3) and sig.shape == (ncols, 37, 2)
     for c in range(ncols):
+        # mixed precision: the single-column pass sums in double-float (about 2^-47
+        # per operation), the multi-column pass in FP64
         Ec, Hc = sim.eval_fields(P, col=c)
-        assert _rel(E[c], Ec) < 1e-12 and _rel(H[c], Hc) < 1e-12
-        assert _rel(sig[c], sim.rcs_points(10.0, th, ph, col=c)) < 1e-12
+        assert _rel(E[c], Ec) < 1e-11 and _rel(H[c], Hc) < 1e-11
+        assert _rel(sig[c], sim.rcs_points(10.0, th, ph, col=c)) < 1e-11
     E2, H2 = sim.eval_fields_multi(P, col0=2, ncols=3, want_h=False)
     assert H2 is None and _rel(E2, E[2:5]) < 1e-15

@@ -48,8 +48,9 @@ def test_sweep_equals_single_frequency_calls(gpu_lib, bowtie500, precision):
     for i, f in enumerate(freqs):
         I, pv, E = _single(ref, f, pts)
         np.testing.assert_array_equal(out["I"][i], I)
-        # the sweep evaluates all columns in one multi-column field pass
-        assert np.abs(out["E"][i] - E).max() <= 1e-12 * np.abs(E).max()
+        # the sweep evaluates all columns in one multi-column field pass (FP64); the
+        # single-column calls of the mixed path sum in double-float (2^-47 per operation)
+        assert np.abs(out["E"][i] - E).max() <= 1e-11 * np.abs(E).max()
         assert out["port"][i]["impedance"] == pv["impedance"]
 
 
