@@ -279,9 +279,17 @@ struct TcPanel {
     float* Ubl;
     int rest, KP;
 };
+// U11^-1 as the B^ and L11^-1 as the A* operand (hi, lo), written by the diagonal-block kernel.
+struct TcDiagSplit {
+    float* uh;
+    float* ul;
+    float* lh;
+    float* ll;
+};
 size_t tc_panel_ws_bytes(int64_t n);
-int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, const float2* Uinv,
-                const float2* Linv, TcPanel* out);
+int tc_diag_split_slots(frico_gpu_ctx* ctx, TcDiagSplit* out);
+int tc_lu_panel_split(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest);
+int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, TcPanel* out);
 int tc_lu_update(frico_gpu_ctx* ctx, const TcPanel& pn, float2* C, int64_t ldc, int boff, int ncols, int max_ctas,
                  cudaEvent_t* ev);   // gemm_tc.cu
 int gemm_update_simt32(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,

@@ -595,47 +595,89 @@ static const int kPanelKP = 256;   // K = 128 complex columns
 
 static size_t al1k(size_t floats) { return (floats + 255) & ~size_t(255); }   // keep slots 1 KB aligned
 
+// Fixed slots (sized for rest = n - 128): U11^-1 (B^), L11^-1 (A*) from the
+// diagonal-block kernel; A21 (A*), A12 (B^) from tc_lu_panel_split; L21 (A*),
+// U12 (B^) from the panel GEMM's epilogue. Each hi then lo.
+struct PanelSlots {
+    float *uh, *ul, *lh, *ll, *a21h, *a21l, *a12h, *a12l, *lah, *lal, *ubh, *ubl;
+};
+
+static PanelSlots panel_slots(void* ws, int64_t n) {
+    const size_t r = size_t(std::max<int64_t>(n - 128, 0)), KP = kPanelKP;
+    float* base = (float*)(((uintptr_t)ws + 1023) & ~uintptr_t(1023));
+    auto take = [&](size_t floats) { float* p = base; base += al1k(floats); return p; };
+    PanelSlots s;
+    s.uh = take(128 * KP);
+    s.ul = take(128 * KP);
+    s.lh = take(256 * KP);
+    s.ll = take(256 * KP);
+    s.a21h = take(2 * r * KP);
+    s.a21l = take(2 * r * KP);
+    s.a12h = take(r * KP);
+    s.a12l = take(r * KP);
+    s.lah = take(2 * r * KP);
+    s.lal = take(2 * r * KP);
+    s.ubh = take(r * KP);
+    s.ubl = take(r * KP);
+    return s;
+}
+
 size_t tc_panel_ws_bytes(int64_t n) {
     const size_t r = size_t(std::max<int64_t>(n - 128, 0)), KP = kPanelKP;
-    // A21 (A*), Uinv (B^), Linv (A*), A12 (B^), L21 (A*), U12 (B^): hi and lo each
     return sizeof(float) * 2 * (2 * al1k(2 * r * KP) + 2 * al1k(r * KP) + al1k(128 * KP) + al1k(256 * KP)) + 4096;
 }
 
+int tc_diag_split_slots(frico_gpu_ctx* ctx, TcDiagSplit* out) {
+    int rc;
+    if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
+    const PanelSlots s = panel_slots(ctx->tc_ws.p, ctx->n);
+    out->uh = s.uh;
+    out->ul = s.ul;
+    out->lh = s.lh;
+    out->ll = s.ll;
+    return FRICO_GPU_OK;
+}
+
+// A21 (rest x 128, below the diagonal block) as A* and A12 (128 x rest, right of it)
+// as B^ operands of the panel GEMM; independent of the diagonal block's factors.
+int tc_lu_panel_split(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest) {
+    const int KP = kPanelKP;
+    if (jb != 128 || rest <= 0) return set_err(ctx, FRICO_GPU_EINVAL, "tc_lu_panel_split: block of 128 expected");
+    int rc;
+    if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
+    const PanelSlots s = panel_slots(ctx->tc_ws.p, ctx->n);
+    float2* A21 = A + int64_t(k0) * lda + k0 + jb;
+    float2* A12 = A + int64_t(k0 + jb) * lda + k0;
+    const tc::SplitPart parts[2] = {split_part(false, A21, lda, rest, jb, s.a21h, s.a21l, KP),
+                                    split_part(true, A12, lda, rest, jb, s.a12h, s.a12l, KP)};
+    return launch_split(ctx, ctx->stream, parts, 2, KP);
+}
+
 // L21 = A21 U11^{-1} and U12 = L11^{-1} A12 (in place in A, jb = 128 columns /
-// rows, rest = rows of A21 = columns of A12) as one launch after one split
-// launch; their epilogues also write L21 as the A* and U12 as the B^ operand of
-// the block column's trailing updates (tc_lu_update).
-int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, const float2* Uinv,
-                const float2* Linv, TcPanel* out) {
+// rows, rest = rows of A21 = columns of A12) as one launch from the split operands
+// (tc_lu_panel_split, and the diagonal-block kernel for U11^{-1}, L11^{-1}); the
+// epilogues also write L21 as the A* and U12 as the B^ operand of the block
+// column's trailing updates (tc_lu_update).
+int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, TcPanel* out) {
     const int KP = kPanelKP;
     if (jb != 128 || rest <= 0) return set_err(ctx, FRICO_GPU_EINVAL, "tc_lu_panel: block of 128 expected");
     int rc;
     if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
-    const size_t r = size_t(rest);
-    float* base = (float*)(((uintptr_t)ctx->tc_ws.p + 1023) & ~uintptr_t(1023));
-    auto take = [&](size_t floats) { float* p = base; base += al1k(floats); return p; };
-    float* a21h = take(2 * r * KP); float* a21l = take(2 * r * KP);
-    float* uih = take(128 * KP);    float* uil = take(128 * KP);
-    float* lih = take(256 * KP);    float* lil = take(256 * KP);
-    float* a12h = take(r * KP);     float* a12l = take(r * KP);
-    out->Lah = take(2 * r * KP);    out->Lal = take(2 * r * KP);
-    out->Ubh = take(r * KP);        out->Ubl = take(r * KP);
+    const PanelSlots s = panel_slots(ctx->tc_ws.p, ctx->n);
+    out->Lah = s.lah;
+    out->Lal = s.lal;
+    out->Ubh = s.ubh;
+    out->Ubl = s.ubl;
     out->rest = rest;
     out->KP = KP;
-    cudaStream_t st = ctx->stream;
     float2* A21 = A + int64_t(k0) * lda + k0 + jb;
     float2* A12 = A + int64_t(k0 + jb) * lda + k0;
-    const tc::SplitPart parts[4] = {split_part(false, A21, lda, rest, jb, a21h, a21l, KP),
-                                    split_part(true, Uinv, 128, jb, jb, uih, uil, KP),
-                                    split_part(false, Linv, 128, jb, jb, lih, lil, KP),
-                                    split_part(true, A12, lda, rest, jb, a12h, a12l, KP)};
-    if ((rc = launch_split(ctx, st, parts, 4, KP))) return rc;
     TcProblem q[2];
-    if ((rc = make_problem(ctx, q[0], A21, lda, 2 * rest, jb, a21h, a21l, uih, uil, KP, 0, 1, out->Lah, out->Lal)))
+    if ((rc = make_problem(ctx, q[0], A21, lda, 2 * rest, jb, s.a21h, s.a21l, s.uh, s.ul, KP, 0, 1, s.lah, s.lal)))
         return rc;
-    if ((rc = make_problem(ctx, q[1], A12, lda, 2 * jb, rest, lih, lil, a12h, a12l, KP, 0, 2, out->Ubh, out->Ubl)))
+    if ((rc = make_problem(ctx, q[1], A12, lda, 2 * jb, rest, s.lh, s.ll, s.a12h, s.a12l, KP, 0, 2, s.ubh, s.ubl)))
         return rc;
-    return launch_gemm(ctx, st, q, 2, KP, 0, nullptr);
+    return launch_gemm(ctx, ctx->stream, q, 2, KP, 0, nullptr);
 }
 
 // C[rest x ncols] -= L21 U12[:, boff : boff + ncols] from the operands tc_lu_panel wrote.

@@ -141,9 +141,19 @@ template <typename C> constexpr size_t diag_lu_smem() { return sizeof(C) * (size
 // CTA 1 writes the LU to A and L^{-1}, CTA 0 U^{-1}; both read the block from
 // `src`, a copy made before the launch (ld 128), so CTA 1 may overwrite A
 // whatever the other's timing.
+// With usplit / lsplit (complex64 only): U^{-1} also as the hi/lo TF32 B^ operand
+// of L21 = A21 U^{-1} (row j = column j of U^{-1}, 256 floats: the hi/lo of the
+// column-major array itself), L^{-1} as the A* operand of U12 = L^{-1} A12
+// (rows 2r = (re, -im), 2r + 1 = (im, re) of row r, 256 floats each).
+__device__ __forceinline__ float2 tf32_hi2(float2 v) {
+    return make_float2(__uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u),
+                       __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u));
+}
+
 template <typename C>
 __global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0, int jb,
-                                                C* Uinv, C* Linv, DeviceStatus* st) {
+                                                C* Uinv, C* Linv, DeviceStatus* st, float2* usplit_h,
+                                                float2* usplit_l, float2* lsplit_h, float2* lsplit_l) {
     using R = decltype(A[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
     C* S = (C*)smraw;              // S[c * kDLD + r]
@@ -187,6 +197,20 @@ __global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A
             const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
             Linv[c * kNP + r] = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
         }
+        if (lsplit_h) {
+#pragma unroll 4
+            for (int it = 0; it < kNP * kNP / 256; it++) {   // A* rows 2r, 2r + 1 at K = 2c, 2c + 1
+                const int idx = threadIdx.x + 256 * it, c = idx & (kNP - 1), r = idx >> 7;
+                const C v = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
+                const float2 a0 = make_float2(float(v.x), -float(v.y)), a1 = make_float2(float(v.y), float(v.x));
+                const float2 h0 = tf32_hi2(a0), h1 = tf32_hi2(a1);
+                const int64_t o0 = int64_t(2 * r) * kNP + c, o1 = o0 + kNP;   // float2 units, rows of 256 floats
+                lsplit_h[o0] = h0;
+                lsplit_h[o1] = h1;
+                lsplit_l[o0] = make_float2(a0.x - h0.x, a0.y - h0.y);
+                lsplit_l[o1] = make_float2(a1.x - h1.x, a1.y - h1.y);
+            }
+        }
     } else {
         diag_sweep<false>(v, S, vb, tx, ty, k0, st);
         __syncthreads();   // S no longer read: it takes U^{-1} (upper triangle and diagonal of W)
@@ -199,7 +223,13 @@ __global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A
 #pragma unroll 8
         for (int it = 0; it < kNP * kNP / 256; it++) {
             const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
-            Uinv[c * kNP + r] = r <= c ? S[c * kDLD + r] : cmake(R(0), R(0));
+            const C v = r <= c ? S[c * kDLD + r] : cmake(R(0), R(0));
+            Uinv[c * kNP + r] = v;
+            if (usplit_h) {
+                const float2 a = make_float2(float(v.x), float(v.y)), h = tf32_hi2(a);
+                usplit_h[c * kNP + r] = h;
+                usplit_l[c * kNP + r] = make_float2(a.x - h.x, a.y - h.y);
+            }
         }
     }
 }
@@ -355,9 +385,11 @@ template <typename C> __global__ void k_copy_block(const C* __restrict__ A, int6
 
 // Copy of the diagonal block, then the two-CTA factor + inverses.
 static int launch_diag_lu(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_t lda, int k0, int jb,
-                          float2* Uinv, float2* Linv, float2* blk, DeviceStatus* dst) {
+                          float2* Uinv, float2* Linv, float2* blk, DeviceStatus* dst, const TcDiagSplit* sp = nullptr) {
     k_copy_block<float2><<<16, 256, 0, st>>>(A, lda, k0, jb, blk);
-    k_diag_lu<float2><<<2, 256, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv, dst);
+    k_diag_lu<float2><<<2, 256, diag_lu_smem<float2>(), st>>>(
+        blk, A, lda, k0, jb, Uinv, Linv, dst, sp ? (float2*)sp->uh : nullptr, sp ? (float2*)sp->ul : nullptr,
+        sp ? (float2*)sp->lh : nullptr, sp ? (float2*)sp->ll : nullptr);
     count_launch(ctx, 2);
     return cuda_check(ctx, cudaGetLastError(), "k_diag_lu");
 }
@@ -484,17 +516,22 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
             cudaStream_t s2 = ctx->stream2;
             cudaEvent_t ev_narrow = ctx->la_ev[0], ev_diag = ctx->la_ev[1];
-            if ((rc = launch_diag_lu(ctx, st, A, lda, 0, std::min(kNP, n), Uinv_of(0), Linv_of(0), Blk, dst))) return rc;
+            TcDiagSplit dsp;
+            if ((rc = tc_diag_split_slots(ctx, &dsp))) return rc;
+            if ((rc = launch_diag_lu(ctx, st, A, lda, 0, std::min(kNP, n), Uinv_of(0), Linv_of(0), Blk, dst, &dsp)))
+                return rc;
+            if (n > kNP && (rc = tc_lu_panel_split(ctx, A, lda, 0, kNP, n - kNP))) return rc;
             bool diag_on_s2 = false;
             for (int k0 = 0; k0 < n; k0 += kNP) {
                 const int jb = std::min(kNP, n - k0);
                 const int rest = n - k0 - jb;
                 if (diag_on_s2 && (rc = cuda_check(ctx, cudaStreamWaitEvent(st, ev_diag, 0), "wait diag"))) return rc;
                 if (rest == 0) break;
-                // L21 = A21 U11^{-1}, U12 = L11^{-1} A12 on the tensor cores, one launch that
-                // also writes both as the operands of the updates below
+                // L21 = A21 U11^{-1}, U12 = L11^{-1} A12 on the tensor cores, one launch (A21 and
+                // A12 were split before the wait above, U11^{-1} and L11^{-1} by the diagonal-block
+                // kernel) that also writes both as the operands of the updates below
                 TcPanel pn;
-                if ((rc = tc_lu_panel(ctx, A, lda, k0, jb, rest, Uinv_of(k0), Linv_of(k0), &pn))) return rc;
+                if ((rc = tc_lu_panel(ctx, A, lda, k0, jb, rest, &pn))) return rc;
                 // trailing update, next block column first; that block's LU then runs on the
                 // second stream while the rest of the update (on all but two SMs) proceeds
                 const int jb1 = std::min(kNP, rest);
@@ -507,7 +544,8 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                 if ((rc = tc_lu_update(ctx, pn, Cm, lda, 0, jb1, 0, ev))) return rc;
                 if ((rc = cuda_check(ctx, cudaEventRecord(ev_narrow, st), "record"))) return rc;
                 if ((rc = cuda_check(ctx, cudaStreamWaitEvent(s2, ev_narrow, 0), "wait narrow"))) return rc;
-                if ((rc = launch_diag_lu(ctx, s2, A, lda, k0 + jb, jb1, Uinv_of(k0 + jb), Linv_of(k0 + jb), Blk, dst)))
+                if ((rc = launch_diag_lu(ctx, s2, A, lda, k0 + jb, jb1, Uinv_of(k0 + jb), Linv_of(k0 + jb), Blk, dst,
+                                         &dsp)))
                     return rc;
                 if ((rc = cuda_check(ctx, cudaEventRecord(ev_diag, s2), "record"))) return rc;
                 diag_on_s2 = true;
@@ -520,6 +558,9 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                     }
                     if ((rc = tc_lu_update(ctx, pn, Cm + int64_t(jb1) * lda, lda, jb1, nr, std::max(1, sms - 2), ev)))
                         return rc;
+                    // the next block column's A21 and A12 are final now: split them while its
+                    // diagonal block is still being factored on the second stream
+                    if ((rc = tc_lu_panel_split(ctx, A, lda, k0 + jb, jb1, nr))) return rc;
                 }
                 if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
             }
