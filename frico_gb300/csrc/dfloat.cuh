@@ -124,4 +124,22 @@ __device__ __forceinline__ bool df_sincos(dfl x, dfl& s, dfl& c) {
     return true;
 }
 
+// complex double-float
+struct cdf {
+    dfl r, i;
+};
+__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
+    return cdf{df_add(df_mul(a.r, b.r), df_neg(df_mul(a.i, b.i))), df_add(df_mul(a.r, b.i), df_mul(a.i, b.r))};
+}
+__device__ __forceinline__ cdf cdf_scale(cdf a, dfl s) { return cdf{df_mul(a.r, s), df_mul(a.i, s)}; }
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return cdf{df_add(a.r, b.r), df_add(a.i, b.i)}; }
+__device__ __forceinline__ cdf cdf_sub(cdf a, cdf b) { return cdf{df_add(a.r, df_neg(b.r)), df_add(a.i, df_neg(b.i))}; }
+__device__ __forceinline__ cdf cdf_of(float4 q) { return cdf{dmk(q.x, q.y), dmk(q.z, q.w)}; }
+__device__ __forceinline__ float4 f4_of(double2 z, int& bad) {
+    float4 q;
+    split_df(z.x, q.x, q.y, bad);
+    split_df(z.y, q.z, q.w, bad);
+    return q;
+}
+
 }  // namespace frico

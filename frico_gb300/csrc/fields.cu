@@ -196,23 +196,6 @@ __global__ void __launch_bounds__(kFP) k_fields_part(int64_t npts, const double*
 // gg = -(1 + jkR) exp(+-jkR) / (4 pi R^3). Currents are split once per triangle
 // when staged. A pair outside the double-float range (kR >= 6400, R^2 beyond
 // the split's exponents) is summed in FP64.
-struct cdf {
-    dfl r, i;
-};
-__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
-    return cdf{df_add(df_mul(a.r, b.r), df_neg(df_mul(a.i, b.i))), df_add(df_mul(a.r, b.i), df_mul(a.i, b.r))};
-}
-__device__ __forceinline__ cdf cdf_scale(cdf a, dfl s) { return cdf{df_mul(a.r, s), df_mul(a.i, s)}; }
-__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return cdf{df_add(a.r, b.r), df_add(a.i, b.i)}; }
-__device__ __forceinline__ cdf cdf_sub(cdf a, cdf b) { return cdf{df_add(a.r, df_neg(b.r)), df_add(a.i, df_neg(b.i))}; }
-__device__ __forceinline__ cdf cdf_of(float4 q) { return cdf{dmk(q.x, q.y), dmk(q.z, q.w)}; }
-__device__ __forceinline__ float4 f4_of(double2 z, int& bad) {
-    float4 q;
-    split_df(z.x, q.x, q.y, bad);
-    split_df(z.y, q.z, q.w, bad);
-    return q;
-}
-
 template <bool WITH_H>
 __global__ void __launch_bounds__(kFP) k_fields_part_df(int64_t npts, const double* __restrict__ P, int64_t nt,
                                                        int64_t tri_per_chunk, const TriGeo* __restrict__ geo,

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace frico {
 
@@ -126,6 +127,151 @@ __global__ void __launch_bounds__(kMP) k_fields_multi(int64_t npts, const double
     }
 }
 
+// The same in double-float for the mixed path (dfloat.cuh): R^2 from FP64
+// differences, then sqrt, 1/R, sincos(kR) and every product and sum in
+// double-float; currents split once per staged triangle. A pair outside the
+// double-float range (kR >= 6400, R^2 beyond the split's exponents) is summed in FP64.
+template <bool WITH_H>
+__global__ void __launch_bounds__(kMP) k_fields_multi_df(int64_t npts, const double* __restrict__ P, int64_t nt,
+                                                         int64_t tri_per_chunk, const TriGeo* __restrict__ geo,
+                                                         const double2* __restrict__ AJ, const double2* __restrict__ AD,
+                                                         int ncols, double k, double omega, int hphase_physical,
+                                                         double2* __restrict__ part) {
+    __shared__ double sc[kMT][3];
+    __shared__ float4 sj[kMT][kRT][4];
+    __shared__ int s_bad[kMT];
+    const int64_t p = blockIdx.x * int64_t(kMP) + threadIdx.x;
+    const int c0 = blockIdx.z * kRT;
+    const int64_t t0 = blockIdx.y * tri_per_chunk, t1 = min(nt, t0 + tri_per_chunk);
+    double px = 0, py = 0, pz = 0;
+    if (p < npts) { px = P[3 * p]; py = P[3 * p + 1]; pz = P[3 * p + 2]; }
+    int kb = 0;
+    const dfl kd = df_from_double(k, kb), invk = df_from_double(1.0 / k, kb);
+    const dfl wmu = df_from_double(omega * FRICO_MU0, kb), inv4pi = df_from_double(0.25 * M_1_PI, kb);
+    const dfl zero = dmk(0.f);
+    cdf E[kRT][3], H[kRT][3];
+#pragma unroll
+    for (int r = 0; r < kRT; r++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) E[r][a] = H[r][a] = cdf{zero, zero};
+    const double2 mjwmu = make_double2(-0.0 * FRICO_MU0, -omega * FRICO_MU0);
+    const double invk2 = 1.0 / (k * k);
+    for (int64_t tb = t0; tb < t1; tb += kMT) {
+        const int cnt = int(min(int64_t(kMT), t1 - tb));
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += kMP) {
+            const double* c = geo[tb + q].c;
+            sc[q][0] = c[0];
+            sc[q][1] = c[1];
+            sc[q][2] = c[2];
+            int bad = 0;
+#pragma unroll
+            for (int r = 0; r < kRT; r++) {
+                const int col = c0 + r;
+                if (col < ncols) {
+                    const double2* aj = AJ + (int64_t(col) * nt + tb + q) * 3;
+                    sj[q][r][0] = f4_of(aj[0], bad);
+                    sj[q][r][1] = f4_of(aj[1], bad);
+                    sj[q][r][2] = f4_of(aj[2], bad);
+                    sj[q][r][3] = f4_of(AD[int64_t(col) * nt + tb + q], bad);
+                } else {
+                    sj[q][r][0] = sj[q][r][1] = sj[q][r][2] = sj[q][r][3] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+            s_bad[q] = bad;
+        }
+        __syncthreads();
+        if (p < npts)
+            for (int q = 0; q < cnt; q++) {
+                const double vx = px - sc[q][0], vy = py - sc[q][1], vz = pz - sc[q][2];
+                const double r2 = fma(vx, vx, fma(vy, vy, vz * vz));
+                int bad = kb;
+                const dfl v[3] = {df_from_double(vx, bad), df_from_double(vy, bad), df_from_double(vz, bad)};
+                const dfl R = df_sqrt(df_from_double(r2, bad));
+                dfl sn, cs;
+                if (!bad && !s_bad[q] && df_sincos(df_mul(kd, R), sn, cs)) {
+                    const dfl invR = df_rcp(R), i4R = df_mul(invR, inv4pi);
+                    const cdf g{df_mul(cs, i4R), df_neg(df_mul(sn, i4R))};
+                    const cdf c1{df_mul(wmu, g.i), df_neg(df_mul(wmu, g.r))};   // -j w mu g
+                    const dfl ikR = df_mul(invR, invk), kR = df_mul(kd, R);
+                    // m = -c1 (1 + jkR) / (kR)^2
+                    const cdf m = cdf_scale(cdf_mul(c1, cdf{dmk(-1.f), df_neg(kR)}), df_mul(ikR, ikR));
+                    const cdf c2[3] = {cdf_scale(m, v[0]), cdf_scale(m, v[1]), cdf_scale(m, v[2])};
+                    cdf gv[3];
+                    if (WITH_H) {
+                        const dfl i4R3 = df_mul(i4R, df_mul(invR, invR));
+                        const cdf ph{cs, hphase_physical ? df_neg(sn) : sn};
+                        const cdf gg = cdf_scale(cdf_mul(cdf{dmk(-1.f), df_neg(kR)}, ph), i4R3);
+#pragma unroll
+                        for (int a = 0; a < 3; a++) gv[a] = cdf_scale(gg, v[a]);
+                    }
+#pragma unroll
+                    for (int r = 0; r < kRT; r++) {
+                        const cdf J0 = cdf_of(sj[q][r][0]), J1 = cdf_of(sj[q][r][1]), J2 = cdf_of(sj[q][r][2]);
+                        const cdf D = cdf_of(sj[q][r][3]);
+                        const cdf Jv[3] = {J0, J1, J2};
+#pragma unroll
+                        for (int a = 0; a < 3; a++) E[r][a] = cdf_add(E[r][a], cdf_add(cdf_mul(c1, Jv[a]), cdf_mul(c2[a], D)));
+                        if (WITH_H) {
+                            H[r][0] = cdf_add(H[r][0], cdf_sub(cdf_mul(gv[1], J2), cdf_mul(gv[2], J1)));
+                            H[r][1] = cdf_add(H[r][1], cdf_sub(cdf_mul(gv[2], J0), cdf_mul(gv[0], J2)));
+                            H[r][2] = cdf_add(H[r][2], cdf_sub(cdf_mul(gv[0], J1), cdf_mul(gv[1], J0)));
+                        }
+                    }
+                } else {
+                    // FP64 (as k_fields_multi), added into the double-float sums
+                    const double R64 = sqrt(r2), invR = 1.0 / R64, i4R = invR * (0.25 * M_1_PI), kR = k * R64;
+                    double s, c;
+                    sincos(kR, &s, &c);
+                    const double2 g = make_double2(c * i4R, -s * i4R);
+                    const double2 c1 = cmul(mjwmu, g);
+                    const double2 m = cscale(cmul(c1, make_double2(1.0, kR)), -(invR * invR * invk2));
+                    const double vr[3] = {vx, vy, vz};
+                    double2 gv[3];
+                    if (WITH_H) {
+                        const double i4R3 = i4R * invR * invR;
+                        const double2 ph = hphase_physical ? make_double2(c, -s) : make_double2(c, s);
+                        const double2 gg = cmul(make_double2(-i4R3, -kR * i4R3), ph);
+                        for (int a = 0; a < 3; a++) gv[a] = cscale(gg, vr[a]);
+                    }
+#pragma unroll
+                    for (int r = 0; r < kRT; r++) {
+                        const int col = c0 + r;
+                        if (col >= ncols) continue;
+                        const double2* aj = AJ + (int64_t(col) * nt + tb + q) * 3;
+                        const double2 Jv[3] = {aj[0], aj[1], aj[2]};
+                        const double2 D = AD[int64_t(col) * nt + tb + q];
+                        int b2 = 0;
+                        for (int a = 0; a < 3; a++) {
+                            const double2 e = cadd(cmul(c1, Jv[a]), cmul(cscale(m, vr[a]), D));
+                            E[r][a] = cdf_add(E[r][a], cdf_of(f4_of(e, b2)));
+                        }
+                        if (WITH_H) {
+                            const double2 h[3] = {csub(cmul(gv[1], Jv[2]), cmul(gv[2], Jv[1])),
+                                                  csub(cmul(gv[2], Jv[0]), cmul(gv[0], Jv[2])),
+                                                  csub(cmul(gv[0], Jv[1]), cmul(gv[1], Jv[0]))};
+                            for (int a = 0; a < 3; a++) H[r][a] = cdf_add(H[r][a], cdf_of(f4_of(h[a], b2)));
+                        }
+                    }
+                }
+            }
+    }
+    if (p < npts) {
+        const int nper = WITH_H ? 6 : 3;
+#pragma unroll
+        for (int r = 0; r < kRT; r++) {
+            const int col = c0 + r;
+            if (col >= ncols) continue;
+            double2* o = part + ((int64_t(blockIdx.y) * ncols + col) * npts + p) * nper;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                o[a] = make_double2(df_to_double(E[r][a].r), df_to_double(E[r][a].i));
+                if (WITH_H) o[3 + a] = make_double2(df_to_double(H[r][a].r), df_to_double(H[r][a].i));
+            }
+        }
+    }
+}
+
 // out[(col * npts + p) * nper + x] = sum over chunks (fixed order)
 __global__ void k_fields_multi_reduce(int64_t cnt, int nchunks, const double2* __restrict__ part,
                                       double2* __restrict__ out) {
@@ -183,12 +329,16 @@ int eval_fields_multi(frico_gpu_ctx* ctx, int col0, int ncols, int64_t npts, con
     const double k = omega * std::sqrt(FRICO_MU0 * FRICO_EPS0);
     const dim3 grid = dim3(unsigned(pblocks), unsigned(nchunks), unsigned(ctiles));
     const int hp = ctx->opt.h_phase_mode == FRICO_HPHASE_PHYSICAL;
-    if (with_h)
-        k_fields_multi<true><<<grid, kMP, 0, st>>>(npts, dP, nt, tpc, (const TriGeo*)ctx->trigeo.p, AJ, AD, ncols, k,
-                                                   omega, hp, part);
+    const TriGeo* geo = (const TriGeo*)ctx->trigeo.p;
+    const bool df = ctx->opt.precision == FRICO_PREC_MIXED;   // double-float on the mixed path
+    if (df && with_h)
+        k_fields_multi_df<true><<<grid, kMP, 0, st>>>(npts, dP, nt, tpc, geo, AJ, AD, ncols, k, omega, hp, part);
+    else if (df)
+        k_fields_multi_df<false><<<grid, kMP, 0, st>>>(npts, dP, nt, tpc, geo, AJ, AD, ncols, k, omega, hp, part);
+    else if (with_h)
+        k_fields_multi<true><<<grid, kMP, 0, st>>>(npts, dP, nt, tpc, geo, AJ, AD, ncols, k, omega, hp, part);
     else
-        k_fields_multi<false><<<grid, kMP, 0, st>>>(npts, dP, nt, tpc, (const TriGeo*)ctx->trigeo.p, AJ, AD, ncols,
-                                                    k, omega, hp, part);
+        k_fields_multi<false><<<grid, kMP, 0, st>>>(npts, dP, nt, tpc, geo, AJ, AD, ncols, k, omega, hp, part);
     k_fields_multi_reduce<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, int(nchunks), part, out);
     count_launch(ctx, 2);
     if ((rc = cuda_check(ctx, cudaGetLastError(), "fields_multi kernels"))) return rc;

@@ -212,12 +212,15 @@ def test_double_float_fields_match_fp64(gpu_lib):
     for prec in ("mixed", "fp64"):
         sim = Simulation(m, precision=prec)
         sim.compute_matrix(f)
-        sim.set_nrhs(1)
-        sim.update_rhs(f, PlaneWave(0.4, 1.1, 1.0, 0.5))
+        sim.set_nrhs(3)
+        for c, pw in enumerate([PlaneWave(0.4, 1.1, 1.0, 0.5), PlaneWave(1.3, 0.2, 0.0, 1.0), PlaneWave(2.0, 2.5, 1.0, 0.0)]):
+            sim.update_rhs(f, pw, c)
         sim.solve()
         Ef, _ = sim.eval_fields(far)
         En, Hn = sim.eval_fields(near)
-        out[prec] = (Ef, En, Hn, sim.bistatic_rcs(10.0))
+        Em, Hm = sim.eval_fields_multi(near)          # the multi-column pass, E and H
+        Efm, _ = sim.eval_fields_multi(far, want_h=False)
+        out[prec] = (Ef, En, Hn, sim.bistatic_rcs(10.0), Em, Hm, Efm)
     for a, b in zip(out["mixed"], out["fp64"]):
         assert rel_norm(a, b) < 1e-9
 
