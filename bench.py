@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--level", type=int, default=4, help="icosphere level (4: N=7680)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 accuracy check")
-    ap.add_argument("--gemm-engine", default="auto", choices=["auto", "simt", "tc"])
+    ap.add_argument("--gemm-engine", default="auto", choices=["auto", "simt", "tc", "tc_f16"],
+                    help="auto/tc: 3xTF32 operands; tc_f16: 3xFP16 block columns of the unpivoted LU")
     ap.add_argument("--pivoting", default="auto", choices=["auto", "partial", "none"])
     ap.add_argument("--workload", default="sphere", choices=["sphere", "strip", "sphere64", "sweep", "adjoint"],
                     help="sphere: one solve per step (headline); sphere64: level-5 sphere, 64 incidences, "
@@ -127,12 +128,12 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def gemm_traffic_per_launch(level: int, precision: str):
+def gemm_traffic_per_launch(level: int, precision: str, kernel: str):
     """DRAM bytes per narrow / trailing-update launch of the complex64 LU from one
     ncu capture (dram__bytes_read.sum + dram__bytes_write.sum over all of a
     solve's update launches), recorded with its command in
-    profiles/k_gemm_tf32x3_sphere_L4_mixed.md; None for other configurations."""
-    p = ROOT / "profiles" / "k_gemm_tf32x3_sphere_L4_mixed.md"
+    profiles/<kernel>_sphere_L4_mixed.md; None for other configurations."""
+    p = ROOT / "profiles" / f"{kernel}_sphere_L4_mixed.md"
     if level != 4 or precision != "mixed" or not p.exists():
         return None
     import re
@@ -193,11 +194,12 @@ def run_reference(args):
 FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (vector and tensor), nominal; no measured figure exists
 
 
-def stage_rooflines(stage, steps, n, nt, npts, iters, green_evals, precision, hbm, bf16):
+def stage_rooflines(stage, steps, n, nt, npts, iters, green_evals, precision, hbm, bf16, f16=False):
     """Per-stage achieved rate against its bound, with the work counts of the
     stage table: fill = Green evaluations x 105 flops (FP64) and Z bytes
-    written; LU = 8/3 N^3; refinement = 16 N^2 bytes of FP64 Z per residual;
-    fields = Nobs Nt (30 + 90) flops (FP64)."""
+    written; LU = 8/3 N^3 (mixed: 3 split products on the tensor cores, FP16
+    at the dense bf16 rate or TF32 at half of it); refinement = 16 N^2 bytes of
+    FP64 Z per residual; fields = Nobs Nt (30 + 90) flops (FP64)."""
     per = {k: v / steps / 1000.0 for k, v in stage.items()}   # seconds per step
     out = {}
     if per["fill_ms"] > 0:
@@ -208,10 +210,12 @@ def stage_rooflines(stage, steps, n, nt, npts, iters, green_evals, precision, hb
                        "z_write_gbs": zb / per["fill_ms"] / 1e9, "hbm_frac": zb / per["fill_ms"] / 1e9 / hbm}
     if per["factor_ms"] > 0:
         t = (8.0 / 3.0) * n ** 3 / per["factor_ms"] / 1e12
+        mixed_peak = bf16 if f16 else bf16 / 2.0
         out["lu"] = {"algorithmic_tflops": t,
-                     "frac": t * (3.0 if precision == "mixed" else 1.0) / (bf16 / 2.0 if precision == "mixed"
+                     "frac": t * (3.0 if precision == "mixed" else 1.0) / (mixed_peak if precision == "mixed"
                                                                             else FP64_NOMINAL_TFLOPS),
-                     "peak": "TF32 = measured bf16 / 2 (3xTF32 does 3 products)" if precision == "mixed"
+                     "peak": ("FP16 = measured bf16 (3xFP16 does 3 products)" if f16 else
+                              "TF32 = measured bf16 / 2 (3xTF32 does 3 products)") if precision == "mixed"
                      else "FP64 nominal"}
     if per["refine_ms"] > 0 and iters and iters[-1] > 0:
         gbs = 16.0 * n * n * iters[-1] / per["refine_ms"] / 1e9
@@ -326,26 +330,30 @@ def run_ours(args):
     hbm, bf16, peak_src = measured_peaks()
     sec = gms / 1000.0 if gms > 0 else float("inf")
     tc = args.precision == "mixed" and args.gemm_engine != "simt"
-    # tensor work of the 3xTF32 path: 3 real GEMMs of (2m x 2k)(2k x n) = 3 x algorithmic complex flops;
-    # TF32 dense peak taken as half of the measured dense bf16 peak
+    # the unpivoted LU's block columns run 3xFP16 when asked for; everything else 3xTF32
+    f16 = tc and args.gemm_engine == "tc_f16" and s1["pivoting_used"] == 2
+    kernel = ("tc::k_gemm_f16x3" if f16 else "tc::k_gemm_tf32x3") if tc else "k_gemm_update<float>"
+    # tensor work of the split path: 3 real GEMMs of (2m x 2k)(2k x n) = 3 x algorithmic complex flops;
+    # FP16 dense peak = the measured dense bf16 peak, TF32 = half of it
     tflops_alg = gfl / sec / 1e12
     tensor_ach = 3.0 * tflops_alg if tc else tflops_alg
-    tensor_peak = bf16 / 2.0 if tc else bf16
+    tensor_peak = (bf16 if f16 else bf16 / 2.0) if tc else bf16
     gbs = gby / sec / 1e9
     frac_t, frac_m = tensor_ach / tensor_peak, gbs / hbm
     if tc and frac_t >= frac_m:
         roof = {"bound": "tensor", "achieved": tensor_ach, "peak": tensor_peak, "unit": "TFLOP/s", "frac": frac_t}
     else:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": frac_m}
-    roof.update({"traffic": gemm_traffic_per_launch(args.level, args.precision) if tc else None,
+    roof.update({"traffic": gemm_traffic_per_launch(args.level, args.precision, kernel.replace("tc::", ""))
+                 if tc else None,
                  "traffic_unit": "bytes per launch (ncu, DRAM read + write)",
                  "algorithmic_bytes_per_launch": gby / max(1, gl),
-                 "kernel": ("tc::k_gemm_tf32x3" if tc else "k_gemm_update<float>") if args.precision == "mixed"
-                 else "k_gemm_update<double>",
+                 "kernel": kernel if args.precision == "mixed" else "k_gemm_update<double>",
                  "launches_per_step": gl / 2, "avg_launch_us": 1000.0 * gms / max(1, gl),
                  "algorithmic_tflops_complex": tflops_alg, "hbm_gbs_algorithmic": gbs,
                  "hbm_frac": frac_m, "tensor_frac": frac_t if tc else None,
-                 "note": f"peaks: hbm {hbm} GB/s, dense bf16 {bf16} TF/s ({peak_src}); TF32 = bf16/2"})
+                 "note": f"peaks: hbm {hbm} GB/s, dense bf16 {bf16} TF/s ({peak_src}); "
+                         + ("FP16 = bf16" if f16 else "TF32 = bf16/2")})
 
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -357,7 +365,7 @@ def run_ours(args):
                        "l2": "working set > L2 (Z 0.94 GB)", "replicas": ws},
             "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
             "stages_roofline": stage_rooflines(stage, args.steps, n, sim.nt, int(T.shape[0]), iters,
-                                               s1["green_evals"], args.precision, hbm, bf16),
+                                               s1["green_evals"], args.precision, hbm, bf16, f16),
             "refine_iters": iters[-1] if iters else 0,
             "pivoting_used": {1: "partial", 2: "none"}.get(s1["pivoting_used"], "?"),
             "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]),

@@ -18,7 +18,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 EDGE_LENGTH_XY, EDGE_LENGTH_TRUE = 0, 1
 HPHASE_COMPAT, HPHASE_PHYSICAL = 0, 1
 GAIN_XY, GAIN_YZ, GAIN_XZ = 0, 1, 2
-GEMM_AUTO, GEMM_SIMT, GEMM_TC = 0, 1, 2
+GEMM_AUTO, GEMM_SIMT, GEMM_TC, GEMM_TC_F16 = 0, 1, 2, 3
 PIVOT_AUTO, PIVOT_PARTIAL, PIVOT_NONE = 0, 1, 2
 REFINE_AUTO, REFINE_CLASSIC = 0, 1
 RESIDUAL_AUTO, RESIDUAL_FP64 = 0, 1

@@ -73,7 +73,7 @@ static int check_options(frico_gpu_ctx* ctx, const frico_gpu_options* o) {
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown precision");
     if (o->h_phase_mode != FRICO_HPHASE_COMPAT && o->h_phase_mode != FRICO_HPHASE_PHYSICAL)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown h_phase_mode");
-    if (o->gemm_engine < FRICO_GEMM_AUTO || o->gemm_engine > FRICO_GEMM_TC)
+    if (o->gemm_engine < FRICO_GEMM_AUTO || o->gemm_engine > FRICO_GEMM_TC_F16)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown gemm_engine");
     if (o->pivoting < FRICO_PIVOT_AUTO || o->pivoting > FRICO_PIVOT_NONE)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown pivoting");
@@ -715,9 +715,9 @@ extern "C" int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, i
                                      const frico_c64* B, frico_c64* C, int32_t engine) {
     FRICO_CTX_CHECK(ctx);
     if (m <= 0 || n <= 0 || k <= 0 || !A || !B || !C) return set_err(ctx, FRICO_GPU_EINVAL, "debug_cgemm: bad args");
-    if (engine != FRICO_GEMM_SIMT && engine != FRICO_GEMM_TC)
-        return set_err(ctx, FRICO_GPU_EINVAL, "debug_cgemm: engine must be SIMT or TC");
-    if (engine == FRICO_GEMM_TC && !gemm_tc_available(ctx))
+    if (engine != FRICO_GEMM_SIMT && engine != FRICO_GEMM_TC && engine != FRICO_GEMM_TC_F16)
+        return set_err(ctx, FRICO_GPU_EINVAL, "debug_cgemm: engine must be SIMT, TC or TC_F16");
+    if (engine != FRICO_GEMM_SIMT && !gemm_tc_available(ctx))
         return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
     int rc;
     if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
@@ -733,8 +733,9 @@ extern "C" int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, i
     if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(dB, B, sizeof(float2) * sb, cudaMemcpyHostToDevice, ctx->stream), "B");
     if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(dC, C, sizeof(float2) * sc, cudaMemcpyHostToDevice, ctx->stream), "C");
     if (!rc)
-        rc = engine == FRICO_GEMM_TC ? gemm_update_tc(ctx, dC, m, dA, m, dB, k, m, n, k, nullptr)
-                                     : gemm_update_simt32(ctx, dC, m, dA, m, dB, k, m, n, k);
+        rc = engine != FRICO_GEMM_SIMT
+                 ? gemm_update_tc(ctx, dC, m, dA, m, dB, k, m, n, k, nullptr, 1, 0, 0, engine == FRICO_GEMM_TC_F16 ? 1 : 0)
+                 : gemm_update_simt32(ctx, dC, m, dA, m, dB, k, m, n, k);
     if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(C, dC, sizeof(float2) * sc, cudaMemcpyDeviceToHost, ctx->stream), "C");
     DeviceStatus hs{};
     if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(&hs, ctx->status.p, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream), "st");

@@ -138,7 +138,7 @@ struct Ctx;
 
 // CUDA graph of the complex64 no-pivot factorisation (see lu_nopiv.cu).
 struct LuGraph {
-    uintptr_t key[10] = {};
+    uintptr_t key[11] = {};
     cudaGraphExec_t exec = nullptr;
     int64_t launches = 0;
     double gemm_flops = 0.0, gemm_bytes = 0.0;
@@ -267,27 +267,37 @@ int trsv128_prepare(frico_gpu_ctx* ctx, cudaStream_t st);             // trsv.cu
 bool gemm_tc_available(frico_gpu_ctx* ctx);                   // gemm_tc.cu
 // C (-)= L U on the tensor cores; max_ctas > 0 caps the persistent grid (leaving
 // SMs to other streams); reuse_a = 1 keeps the operand split of L from the
-// previous call with the same L, m, k.
+// previous call with the same L, m, k; f16 = 1: 3xFP16 operands (else 3xTF32).
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl,
                    const float2* U, int64_t ldu, int m, int n, int k, cudaEvent_t* ev,
-                   int accumulate = 1, int max_ctas = 0, int reuse_a = 0);
+                   int accumulate = 1, int max_ctas = 0, int reuse_a = 0, int f16 = 0);
 // Operands of the no-pivot LU's trailing updates written by tc_lu_panel (gemm_tc.cu).
 struct TcPanel {
-    float* Lah;
-    float* Lal;
-    float* Ubh;
-    float* Ubl;
+    void* Lah;   // float (3xTF32) or __half (3xFP16, h = 1) operands
+    void* Lal;
+    void* Ubh;
+    void* Ubl;
     int rest, KP;
+    int h;
+    const float* sc;   // 3xFP16 operand scale s (device)
 };
-// U11^-1 as the B^ and L11^-1 as the A* operand (hi, lo), written by the diagonal-block kernel.
+// U11^-1 as the B^ and L11^-1 as the A* operand (hi, lo), written by the
+// diagonal-block kernel: TF32 in floats, or (h = 1) FP16, each block scaled by
+// the power of two u (l) that puts its largest entry in [2^8, 2^9); the kernel
+// then writes 1 / (s u) to *res_l21 and 1 / (l s) to *res_u12 (s = *sc).
 struct TcDiagSplit {
-    float* uh;
-    float* ul;
-    float* lh;
-    float* ll;
+    void* uh;
+    void* ul;
+    void* lh;
+    void* ll;
+    int h;
+    const float* sc;
+    float* res_l21;
+    float* res_u12;
 };
 size_t tc_panel_ws_bytes(int64_t n);
 int tc_diag_split_slots(frico_gpu_ctx* ctx, TcDiagSplit* out);
+int tc_lu_scale(frico_gpu_ctx* ctx, const float2* A, int64_t lda, int n);
 int tc_lu_panel_split(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest);
 int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest, TcPanel* out);
 int tc_lu_update(frico_gpu_ctx* ctx, const TcPanel& pn, float2* C, int64_t ldc, int boff, int ncols, int max_ctas,

@@ -10,15 +10,26 @@
 // i.e. the real product lands exactly in the interleaved column-major layout
 // of C, which the epilogue updates in place.
 //
-// Precision: 3xTF32. Every operand x is split into hi = x with the low 13
-// mantissa bits cleared (exactly what the TF32 datapath reads) and
-// lo = x - hi; the MMA chain accumulates hi*hi + hi*lo + lo*hi in FP32, which
-// keeps the update at FP32-level accuracy.
+// Precision: three products of split operands, accumulated in FP32.
+//  3xTF32 (k_gemm_tf32x3): every operand x is split into hi = x with the low 13
+//    mantissa bits cleared (exactly what the TF32 datapath reads) and
+//    lo = x - hi; the MMA chain accumulates hi*hi + hi*lo + lo*hi, which keeps
+//    the update at FP32-level accuracy.
+//  3xFP16 (k_gemm_f16x3, the no-pivot LU's block columns with engine
+//    FRICO_GEMM_TC_F16): hi = fp16(x),
+//    lo = fp16(x - hi). FP16 keeps the same 10 explicit mantissa bits as TF32,
+//    so the three products are as accurate, at twice the MMA rate and half the
+//    operand bytes. Its 5-bit exponent needs scaling: every operand is stored
+//    multiplied by an exact power of two (from the largest |Z| on the diagonal,
+//    so that operands sit near 2^8 and keep 2^-25 of that as absolute floor),
+//    and the epilogue multiplies the accumulator by the inverse power. An
+//    operand beyond the FP16 range becomes infinite; the factorisation then
+//    reports a non-finite pivot and the caller falls back to partial pivoting.
 //
 // Kernel: persistent, warp-specialised, one CTA per SM.
-//   warp 0      TMA producer: per 32-float K slab, the four 128 x 32 operand
-//               tiles (A hi/lo, B hi/lo) into a 3-stage shared-memory ring,
-//               128-byte swizzle.
+//   warp 0      TMA producer: per 128-byte K slab (32 TF32 or 64 FP16 values),
+//               the four 128-row operand tiles (A hi/lo, B hi/lo) into a
+//               3-stage shared-memory ring, 128-byte swizzle.
 //   warp 1      allocates 256 TMEM columns (two 128 x 128 FP32 accumulators)
 //               and issues tcgen05.mma (M = 128, N = 128, K = 8 per
 //               instruction); tcgen05.commit frees ring stages and publishes
@@ -30,6 +41,7 @@
 // All mbarrier waits are bounded; on timeout the CTA records
 // FRICO_DEV_ERR_TIMEOUT in the status word and leaves its loops.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -120,6 +132,19 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
 }
 
+// Instruction descriptor, kind::f16: D = F32, A = B = F16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accum) {
     asm volatile(
@@ -157,13 +182,20 @@ struct GemmProb {
     int M, N;          // real rows (2 x complex rows), columns
     int tiles_m, tiles;
     int accumulate;    // 1: C -= A B; 0: C = A B
-    int emit;          // 0, 1 (A*) or 2 (B^), into eh / el with rows of KP floats
-    float* eh;
-    float* el;
+    int emit;          // 0, 1 (A*) or 2 (B^), into eh / el with rows of KP operand values
+    void* eh;          // float (3xTF32) or __half (3xFP16) operands
+    void* el;
+    // 3xFP16 only: result = accumulator x oc x (*osp)^op, emitted operand =
+    // result x ec x (*esp)^ep, with *osp, *esp device powers of two and op, ep in {-1, 0, 1}
+    const float* osp;
+    const float* esp;
+    float oc, ec;
+    int op, ep;
 };
 
 // Up to two independent problems in one launch (tiles of problem 0, then 1),
-// with the same padded K. KP = padded K in floats (multiple of 32).
+// with the same padded K. KP = padded K in operand values (a multiple of one
+// 128-byte slab: 32 TF32 or 64 FP16).
 struct GemmArgs {
     GemmProb p[2];
     int nprob, KP;
@@ -172,13 +204,26 @@ struct GemmArgs {
 
 __device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
-template <int BN>
-__global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
-    const __grid_constant__ CUtensorMap tmAh0, const __grid_constant__ CUtensorMap tmAl0,
-    const __grid_constant__ CUtensorMap tmBh0, const __grid_constant__ CUtensorMap tmBl0,
-    const __grid_constant__ CUtensorMap tmAh1, const __grid_constant__ CUtensorMap tmAl1,
-    const __grid_constant__ CUtensorMap tmBh1, const __grid_constant__ CUtensorMap tmBl1, GemmArgs g) {
+// hi = fp16(x), lo = fp16(x - hi) (x - hi is exact in FP32)
+__device__ __forceinline__ void split_f16(float x, __half& hi, __half& lo) {
+    hi = __float2half_rn(x);
+    lo = __float2half_rn(x - __half2float(hi));
+}
+
+__device__ __forceinline__ float pow_scale(const float* sc, float c, int p) {
+    if (p == 0) return c;
+    const float s = *sc;
+    return c * (p > 0 ? s : 1.f / s);   // powers of two: exact
+}
+
+// The kernel body for both operand types (H: 3xFP16, else 3xTF32).
+template <int BN, bool H>
+__device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtensorMap& tmAl0,
+                                          const CUtensorMap& tmBh0, const CUtensorMap& tmBl0,
+                                          const CUtensorMap& tmAh1, const CUtensorMap& tmAl1,
+                                          const CUtensorMap& tmBh1, const CUtensorMap& tmBl1, const GemmArgs& g) {
     constexpr int STAGES = Cfg<BN>::STAGES, STAGE_BYTES = Cfg<BN>::STAGE_BYTES;
+    constexpr int BKE = H ? 2 * BK : BK;   // operand values per 128-byte slab
     constexpr int A_TILE = Cfg<BN>::A_TILE, B_TILE = Cfg<BN>::B_TILE, TMEM_COLS = Cfg<BN>::TMEM_COLS;
     static_assert(BN == 2 * 64, "the epilogue gives each of two warps per quadrant 64 columns");
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -194,7 +239,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntiles = g.p[0].tiles + (g.nprob > 1 ? g.p[1].tiles : 0);
-    const int kslabs = g.KP / BK;
+    const int kslabs = g.KP / BKE;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -234,16 +279,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
                     if (!(ok = mbar_wait(&empty[s], (round & 1) ^ 1, g.st))) break;
                     unsigned char* base = ring + s * STAGE_BYTES;
                     mbar_expect_tx(&full[s], STAGE_BYTES);
-                    tma_load_2d(base, mAh, &full[s], ks * BK, mt * BM);
-                    tma_load_2d(base + A_TILE, mAl, &full[s], ks * BK, mt * BM);
-                    tma_load_2d(base + 2 * A_TILE, mBh, &full[s], ks * BK, nt_ * BN);
-                    tma_load_2d(base + 2 * A_TILE + B_TILE, mBl, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base, mAh, &full[s], ks * BKE, mt * BM);
+                    tma_load_2d(base + A_TILE, mAl, &full[s], ks * BKE, mt * BM);
+                    tma_load_2d(base + 2 * A_TILE, mBh, &full[s], ks * BKE, nt_ * BN);
+                    tma_load_2d(base + 2 * A_TILE + B_TILE, mBl, &full[s], ks * BKE, nt_ * BN);
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_tf32(BM, BN);
+            const uint32_t idesc = H ? idesc_f16(BM, BN) : idesc_tf32(BM, BN);
             int it = 0, tcount = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, tcount++) {
@@ -257,16 +302,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t base = smem_u32(ring + s * STAGE_BYTES);
 #pragma unroll
-                    for (int kk = 0; kk < BK / 8; kk++) {
-                        const uint32_t off = uint32_t(kk * 32);   // 8 TF32 = 32 bytes along K
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint32_t off = uint32_t(kk * 32);   // 8 TF32 or 16 FP16 = 32 bytes along K
                         const uint64_t ah = smem_desc_sw128(base + off);
                         const uint64_t al = smem_desc_sw128(base + A_TILE + off);
                         const uint64_t bh = smem_desc_sw128(base + 2 * A_TILE + off);
                         const uint64_t bl = smem_desc_sw128(base + 2 * A_TILE + B_TILE + off);
                         const uint32_t first = (ks == 0 && kk == 0) ? 0u : 1u;
-                        mma_tf32(tmem_d, ah, bh, idesc, first);
-                        mma_tf32(tmem_d, ah, bl, idesc, 1u);
-                        mma_tf32(tmem_d, al, bh, idesc, 1u);
+                        if constexpr (H) {
+                            mma_f16(tmem_d, ah, bh, idesc, first);
+                            mma_f16(tmem_d, ah, bl, idesc, 1u);
+                            mma_f16(tmem_d, al, bh, idesc, 1u);
+                        } else {
+                            mma_tf32(tmem_d, ah, bh, idesc, first);
+                            mma_tf32(tmem_d, ah, bl, idesc, 1u);
+                            mma_tf32(tmem_d, al, bh, idesc, 1u);
+                        }
                     }
                     mma_commit(&empty[s]);
                 }
@@ -290,6 +341,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
             const bool rowok = gr < P.M;
             const int64_t ldc = P.ldc;
             const int accumulate = P.accumulate, emit = P.emit;
+            float osc = 1.f, esc = 1.f;
+            if constexpr (H) {
+                osc = pow_scale(P.osp, P.oc, P.op);
+                esc = pow_scale(P.esp, P.ec, P.ep);
+            }
             float* cp = P.C + int64_t(nt_ * BN + h) * ldc + gr;
             // C values first: these reads do not depend on the accumulator
             float cv[64];
@@ -315,16 +371,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
                 float* stg = staging + (warp - 2) * 1024;   // [row (lane)][column ^ row], 32 x 32
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
-                    const float o = accumulate ? cv[c0 + j] - v[j] : v[j];
+                    const float d = H ? v[j] * osc : v[j];
+                    const float o = accumulate ? cv[c0 + j] - d : d;
                     const bool ok = rowok && c0 + j < ncol;
                     if (ok) wp[int64_t(j) * ldc] = o;
                     if (emit == 1) {
                         stg[lane * 32 + (j ^ lane)] = o;
                     } else if (emit == 2 && ok) {
                         const int64_t off = int64_t(nt_ * BN + h + c0 + j) * g.KP + gr;
-                        const float hi = tf32_hi(o);
-                        P.eh[off] = hi;
-                        P.el[off] = o - hi;
+                        if constexpr (H) {
+                            split_f16(o * esc, ((__half*)P.eh)[off], ((__half*)P.el)[off]);
+                        } else {
+                            const float hi = tf32_hi(o);
+                            ((float*)P.eh)[off] = hi;
+                            ((float*)P.el)[off] = o - hi;
+                        }
                     }
                 }
                 if (emit == 1) {
@@ -339,9 +400,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
                         if (colok && R < P.M) {
                             const float2 w = (i & 1) ? make_float2(a, b) : make_float2(a, -b);
                             const int64_t off = int64_t(R) * g.KP + 2 * col;
-                            const float2 wh = make_float2(tf32_hi(w.x), tf32_hi(w.y));
-                            *reinterpret_cast<float2*>(P.eh + off) = wh;
-                            *reinterpret_cast<float2*>(P.el + off) = make_float2(w.x - wh.x, w.y - wh.y);
+                            if constexpr (H) {
+                                __half2 wh, wl;
+                                split_f16(w.x * esc, wh.x, wl.x);
+                                split_f16(w.y * esc, wh.y, wl.y);
+                                ((__half2*)P.eh)[off >> 1] = wh;
+                                ((__half2*)P.el)[off >> 1] = wl;
+                            } else {
+                                const float2 wh = make_float2(tf32_hi(w.x), tf32_hi(w.y));
+                                *reinterpret_cast<float2*>((float*)P.eh + off) = wh;
+                                *reinterpret_cast<float2*>((float*)P.el + off) = make_float2(w.x - wh.x, w.y - wh.y);
+                            }
                         }
                     }
                     __syncwarp();
@@ -359,11 +428,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
     }
 }
 
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1) k_gemm_tf32x3(
+    const __grid_constant__ CUtensorMap tmAh0, const __grid_constant__ CUtensorMap tmAl0,
+    const __grid_constant__ CUtensorMap tmBh0, const __grid_constant__ CUtensorMap tmBl0,
+    const __grid_constant__ CUtensorMap tmAh1, const __grid_constant__ CUtensorMap tmAl1,
+    const __grid_constant__ CUtensorMap tmBh1, const __grid_constant__ CUtensorMap tmBl1,
+    const __grid_constant__ GemmArgs g) {
+    gemm_body<BN, false>(tmAh0, tmAl0, tmBh0, tmBl0, tmAh1, tmAl1, tmBh1, tmBl1, g);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1) k_gemm_f16x3(
+    const __grid_constant__ CUtensorMap tmAh0, const __grid_constant__ CUtensorMap tmAl0,
+    const __grid_constant__ CUtensorMap tmBh0, const __grid_constant__ CUtensorMap tmBl0,
+    const __grid_constant__ CUtensorMap tmAh1, const __grid_constant__ CUtensorMap tmAl1,
+    const __grid_constant__ CUtensorMap tmBh1, const __grid_constant__ CUtensorMap tmBl1,
+    const __grid_constant__ GemmArgs g) {
+    gemm_body<BN, true>(tmAh0, tmAl0, tmBh0, tmBl0, tmAh1, tmAl1, tmBh1, tmBl1, g);
+}
+
+// Store x as a hi/lo operand pair at element o: TF32 (float arrays) or, with a
+// scale, FP16 (__half arrays).
+__device__ __forceinline__ void put_split(void* hp, void* lp, int64_t o, float x, bool h, float scale) {
+    if (h) {
+        split_f16(x * scale, ((__half*)hp)[o], ((__half*)lp)[o]);
+    } else {
+        const float hi = tf32_hi(x);
+        ((float*)hp)[o] = hi;
+        ((float*)lp)[o] = x - hi;
+    }
+}
+
 // A* hi/lo from the complex panel L (m x k, column-major, lda): rows 2r, 2r+1,
-// KP floats each (zero beyond 2k). A CTA handles 32 complex rows.
+// KP values each (zero beyond 2k). A CTA handles 32 complex rows.
 __device__ __forceinline__ void split_a_tile(int bx, int by, const float2* __restrict__ L, int64_t lda, int m, int k,
-                                             int KP, float* __restrict__ Ah, float* __restrict__ Al,
-                                             float2 (*t)[65]) {
+                                             int KP, void* Ah, void* Al, bool h, float scale, float2 (*t)[65]) {
     const int r0 = bx * 32;
     // by takes one 64-column chunk of K (more CTAs in flight for this store-bound copy)
     for (int q0 = by * 64; q0 < min(KP / 2, (by + 1) * 64); q0 += 64) {
@@ -382,10 +482,7 @@ __device__ __forceinline__ void split_a_tile(int bx, int by, const float2* __res
             if (r >= m || q0 + qq >= KP / 2) continue;
             float2 a = t[rr][qq];
             float x = s == 0 ? (part == 0 ? a.x : -a.y) : (part == 0 ? a.y : a.x);
-            float hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-            int64_t o = int64_t(2 * r + s) * KP + 2 * q0 + col;
-            Ah[o] = hi;
-            Al[o] = x - hi;
+            put_split(Ah, Al, int64_t(2 * r + s) * KP + 2 * q0 + col, x, h, scale);
         }
     }
 }
@@ -393,7 +490,7 @@ __device__ __forceinline__ void split_a_tile(int bx, int by, const float2* __res
 // B^ hi/lo from the complex block U (k x n, column-major, lda): row j = the
 // 2k floats of column j, zero-padded to KP.
 __device__ __forceinline__ void split_b_elem(int64_t idx, const float2* __restrict__ U, int64_t lda, int k, int n,
-                                             int KP, float* __restrict__ Bh, float* __restrict__ Bl) {
+                                             int KP, void* Bh, void* Bl, bool h, float scale) {
     if (idx >= int64_t(n) * KP) return;
     int j = int(idx / KP), c = int(idx % KP);
     float x = 0.f;
@@ -401,9 +498,7 @@ __device__ __forceinline__ void split_b_elem(int64_t idx, const float2* __restri
         const float* col = (const float*)(U + int64_t(j) * lda);
         x = col[c];
     }
-    float hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-    Bh[idx] = hi;
-    Bl[idx] = x - hi;
+    put_split(Bh, Bl, idx, x, h, scale);
 }
 
 // Operand splits of one or two updates in a single launch: up to four parts,
@@ -413,9 +508,13 @@ struct SplitPart {
     const float2* src;
     int64_t ld;
     int rows, k;       // A*: complex rows m; B^: columns n. k: complex K
-    float* hi;
-    float* lo;
+    void* hi;
+    void* lo;
     int isB, a_cols, blocks;
+    int h;             // 1: FP16 operands, value x c x s^p (s = *sc); 0: TF32
+    const float* sc;
+    float c;
+    int p;
 };
 struct SplitArgs {
     SplitPart p[4];
@@ -430,10 +529,12 @@ __global__ void __launch_bounds__(256) k_split_parts(SplitArgs a) {
         i++;
     }
     const SplitPart P = i == 0 ? a.p[0] : i == 1 ? a.p[1] : i == 2 ? a.p[2] : a.p[3];
+    const float scale = P.h ? pow_scale(P.sc, P.c, P.p) : 1.f;
     if (P.isB)
-        split_b_elem(int64_t(b) * blockDim.x + threadIdx.x, P.src, P.ld, P.k, P.rows, a.KP, P.hi, P.lo);
+        split_b_elem(int64_t(b) * blockDim.x + threadIdx.x, P.src, P.ld, P.k, P.rows, a.KP, P.hi, P.lo, P.h != 0,
+                     scale);
     else
-        split_a_tile(b / P.a_cols, b % P.a_cols, P.src, P.ld, P.rows, P.k, a.KP, P.hi, P.lo, t);
+        split_a_tile(b / P.a_cols, b % P.a_cols, P.src, P.ld, P.rows, P.k, a.KP, P.hi, P.lo, P.h != 0, scale, t);
 }
 
 }  // namespace tc
@@ -457,17 +558,19 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// rows x KP floats, row-major (K-major), box box_rows x 32 floats, 128B swizzle.
-static bool make_map(CUtensorMap* m, float* base, int rows, int KP, int box_rows) {
+// rows x KP operand values (FP32, or FP16 with h), row-major (K-major), box
+// box_rows x 128 bytes, 128B swizzle.
+static bool make_map(CUtensorMap* m, const void* base, int rows, int KP, int box_rows, bool h = false) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
+    const uint32_t esz = h ? 2 : 4;
     cuuint64_t dims[2] = {cuuint64_t(KP), cuuint64_t(rows)};
-    cuuint64_t strides[1] = {cuuint64_t(KP) * 4};
-    cuuint32_t box[2] = {uint32_t(tc::BK), uint32_t(box_rows)};
+    cuuint64_t strides[1] = {cuuint64_t(KP) * esz};
+    cuuint32_t box[2] = {128 / esz, uint32_t(box_rows)};
     cuuint32_t es[2] = {1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
-           CUDA_SUCCESS;
+    return fn(m, h ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base),
+              dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 bool gemm_tc_available(frico_gpu_ctx* ctx) {
@@ -477,9 +580,20 @@ bool gemm_tc_available(frico_gpu_ctx* ctx) {
     return major == 10 && minor == 3 && encode_fn() != nullptr;
 }
 
-static tc::SplitPart split_part(bool isB, const float2* src, int64_t ld, int rows, int k, float* hi, float* lo,
-                                int KP) {
+// Operand scaling of a 3xFP16 operand or result: c x s^p, s the power of two at sc.
+struct Pow2Scale {
+    const float* sc;
+    float c;
+    int p;
+};
+
+static tc::SplitPart split_part(bool isB, const float2* src, int64_t ld, int rows, int k, void* hi, void* lo,
+                                int KP, const Pow2Scale* h = nullptr) {
     tc::SplitPart p;
+    p.h = h ? 1 : 0;
+    p.sc = h ? h->sc : nullptr;
+    p.c = h ? h->c : 1.f;
+    p.p = h ? h->p : 0;
     p.src = src;
     p.ld = ld;
     p.rows = rows;
@@ -512,14 +626,24 @@ static int launch_split(frico_gpu_ctx* ctx, cudaStream_t st, const tc::SplitPart
 struct TcProblem {
     CUtensorMap mah, mal, mbh, mbl;
     tc::GemmProb p;
+    bool h;   // 3xFP16 operands
 };
 
-static int make_problem(frico_gpu_ctx* ctx, TcProblem& q, float2* C, int64_t ldc, int M, int N, const float* Ah,
-                        const float* Al, const float* Bh, const float* Bl, int KP, int accumulate, int emit,
-                        float* eh, float* el) {
-    if (!make_map(&q.mah, (float*)Ah, M, KP, tc::BM) || !make_map(&q.mal, (float*)Al, M, KP, tc::BM) ||
-        !make_map(&q.mbh, (float*)Bh, N, KP, 128) || !make_map(&q.mbl, (float*)Bl, N, KP, 128))
+// res / emi (3xFP16 only, both or neither): the result's and the emitted operand's scales.
+static int make_problem(frico_gpu_ctx* ctx, TcProblem& q, float2* C, int64_t ldc, int M, int N, const void* Ah,
+                        const void* Al, const void* Bh, const void* Bl, int KP, int accumulate, int emit,
+                        void* eh, void* el, const Pow2Scale* res = nullptr, const Pow2Scale* emi = nullptr) {
+    const bool h = res != nullptr;
+    if (!make_map(&q.mah, Ah, M, KP, tc::BM, h) || !make_map(&q.mal, Al, M, KP, tc::BM, h) ||
+        !make_map(&q.mbh, Bh, N, KP, 128, h) || !make_map(&q.mbl, Bl, N, KP, 128, h))
         return set_err(ctx, FRICO_GPU_ECUDA, "cuTensorMapEncodeTiled failed");
+    q.h = h;
+    q.p.osp = h ? res->sc : nullptr;
+    q.p.oc = h ? res->c : 1.f;
+    q.p.op = h ? res->p : 0;
+    q.p.esp = emi ? emi->sc : nullptr;
+    q.p.ec = emi ? emi->c : 1.f;
+    q.p.ep = emi ? emi->p : 0;
     q.p.C = (float*)C;
     q.p.ldc = 2 * ldc;
     q.p.M = M;
@@ -537,11 +661,16 @@ static int launch_gemm(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem* q, 
                        cudaEvent_t* ev) {
     int rc;
     if ((rc = device_once(ctx, kOnceGemmTc, [](frico_gpu_ctx* c) {
-             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3<128>,
+             int r = cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_tf32x3<128>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        tc::Cfg<128>::SMEM_BYTES), "tc smem attribute");
+             if (r) return r;
+             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_f16x3<128>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                        tc::Cfg<128>::SMEM_BYTES), "tc smem attribute");
          })))
         return rc;
+    if (np > 1 && q[0].h != q[1].h) return set_err(ctx, FRICO_GPU_EINVAL, "launch_gemm: mixed operand types");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     tc::GemmArgs ga;
@@ -555,38 +684,49 @@ static int launch_gemm(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem* q, 
     const TcProblem& q1 = q[np > 1 ? 1 : 0];
     if (ev) cudaEventRecord(ev[0], st);
     const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
-    tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(
-        q[0].mah, q[0].mal, q[0].mbh, q[0].mbl, q1.mah, q1.mal, q1.mbh, q1.mbl, ga);
+    if (q[0].h)
+        tc::k_gemm_f16x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(
+            q[0].mah, q[0].mal, q[0].mbh, q[0].mbl, q1.mah, q1.mal, q1.mbh, q1.mbl, ga);
+    else
+        tc::k_gemm_tf32x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(
+            q[0].mah, q[0].mal, q[0].mbh, q[0].mbl, q1.mah, q1.mal, q1.mbh, q1.mbl, ga);
     if (ev) cudaEventRecord(ev[1], st);
     count_launch(ctx);
-    return cuda_check(ctx, cudaGetLastError(), "k_gemm_tf32x3");
+    return cuda_check(ctx, cudaGetLastError(), q[0].h ? "k_gemm_f16x3" : "k_gemm_tf32x3");
 }
 
 // C[m x n] -= L[m x k] * U[k x n] (accumulate = 1) or C = L U (accumulate = 0),
 // complex64 column-major, leading dims ldc, ldl, ldu. C may alias L or U: both
-// operands are copied (split) before the MMA kernel writes C.
+// operands are copied (split) before the MMA kernel writes C. f16 = 1: 3xFP16
+// operands (L x 2^6, U x 2^8, for entries of order one), else 3xTF32.
 int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, int64_t ldl, const float2* U,
-                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev, int accumulate, int max_ctas, int reuse_a) {
+                   int64_t ldu, int m, int n, int k, cudaEvent_t* ev, int accumulate, int max_ctas, int reuse_a,
+                   int f16) {
     if (m <= 0 || n <= 0 || k <= 0) return FRICO_GPU_OK;
-    const int KP = ((2 * k + tc::BK - 1) / tc::BK) * tc::BK;
+    const int slab = f16 ? 2 * tc::BK : tc::BK;
+    const int KP = ((2 * k + slab - 1) / slab) * slab;
     const int M = 2 * m;
     const size_t a_elems = size_t(M) * KP, b_elems = size_t(n) * KP;
     int rc;
     const size_t before = ctx->tc_ws.bytes;
     if ((rc = ensure(ctx, ctx->tc_ws, sizeof(float) * 2 * (a_elems + b_elems) + 4096))) return rc;
     if (ctx->tc_ws.bytes != before) reuse_a = 0;   // regrown workspace (even at the same address): split again
-    float* Ah = (float*)(((uintptr_t)ctx->tc_ws.p + 1023) & ~uintptr_t(1023));
-    float* Al = Ah + a_elems;
-    float* Bh = Al + a_elems;
-    float* Bl = Bh + b_elems;
+    const size_t esz = f16 ? 2 : 4;
+    char* Ah = (char*)(((uintptr_t)ctx->tc_ws.p + 1023) & ~uintptr_t(1023));
+    char* Al = Ah + a_elems * esz;
+    char* Bh = Al + a_elems * esz;
+    char* Bl = Bh + b_elems * esz;
     cudaStream_t st = ctx->stream;
+    const Pow2Scale as{nullptr, 64.f, 0}, bs{nullptr, 256.f, 0}, rs{nullptr, 1.f / (64.f * 256.f), 0};
     tc::SplitPart parts[2];
     int np = 0;
-    if (!reuse_a) parts[np++] = split_part(false, L, ldl, m, k, Ah, Al, KP);
-    parts[np++] = split_part(true, U, ldu, n, k, Bh, Bl, KP);
+    if (!reuse_a) parts[np++] = split_part(false, L, ldl, m, k, Ah, Al, KP, f16 ? &as : nullptr);
+    parts[np++] = split_part(true, U, ldu, n, k, Bh, Bl, KP, f16 ? &bs : nullptr);
     if ((rc = launch_split(ctx, st, parts, np, KP))) return rc;
     TcProblem q;
-    if ((rc = make_problem(ctx, q, C, ldc, M, n, Ah, Al, Bh, Bl, KP, accumulate, 0, nullptr, nullptr))) return rc;
+    if ((rc = make_problem(ctx, q, C, ldc, M, n, Ah, Al, Bh, Bl, KP, accumulate, 0, nullptr, nullptr,
+                           f16 ? &rs : nullptr)))
+        return rc;
     return launch_gemm(ctx, st, &q, 1, KP, max_ctas, ev);
 }
 
@@ -595,11 +735,13 @@ static const int kPanelKP = 256;   // K = 128 complex columns
 
 static size_t al1k(size_t floats) { return (floats + 255) & ~size_t(255); }   // keep slots 1 KB aligned
 
-// Fixed slots (sized for rest = n - 128): U11^-1 (B^), L11^-1 (A*) from the
-// diagonal-block kernel; A21 (A*), A12 (B^) from tc_lu_panel_split; L21 (A*),
-// U12 (B^) from the panel GEMM's epilogue. Each hi then lo.
+// Fixed slots (sized for rest = n - 128, 4 bytes per value whichever the
+// operand type): U11^-1 (B^), L11^-1 (A*) from the diagonal-block kernel; A21
+// (A*), A12 (B^) from tc_lu_panel_split; L21 (A*), U12 (B^) from the panel
+// GEMM's epilogue. Each hi then lo. Then the operand scale s of the 3xFP16 form.
 struct PanelSlots {
     float *uh, *ul, *lh, *ll, *a21h, *a21l, *a12h, *a12l, *lah, *lal, *ubh, *ubl;
+    float* scale;   // s, then the result scales of L21 and U12 (written by the diagonal-block kernel)
 };
 
 static PanelSlots panel_slots(void* ws, int64_t n) {
@@ -619,13 +761,58 @@ static PanelSlots panel_slots(void* ws, int64_t n) {
     s.lal = take(2 * r * KP);
     s.ubh = take(r * KP);
     s.ubl = take(r * KP);
+    s.scale = take(3);
     return s;
 }
 
 size_t tc_panel_ws_bytes(int64_t n) {
     const size_t r = size_t(std::max<int64_t>(n - 128, 0)), KP = kPanelKP;
-    return sizeof(float) * 2 * (2 * al1k(2 * r * KP) + 2 * al1k(r * KP) + al1k(128 * KP) + al1k(256 * KP)) + 4096;
+    return sizeof(float) * (2 * (2 * al1k(2 * r * KP) + 2 * al1k(r * KP) + al1k(128 * KP) + al1k(256 * KP)) +
+                            al1k(3)) +
+           4096;
 }
+
+// The block columns use 3xFP16 operands when that engine is asked for, else 3xTF32.
+static bool panel_f16(const frico_gpu_ctx* ctx) { return ctx->opt.gemm_engine == FRICO_GEMM_TC_F16; }
+
+// Scales of the 3xFP16 operands and results, all powers of two:
+//   A21, A12, U12 (Z-sized)   x s, s = 2^(9 - e) with 2^(e-1) <= max |diag Z| < 2^e,
+//                             so that Z-sized values sit in [2^8, 2^9)
+//   L21 (multipliers)         x 2^6
+//   U11^-1, L11^-1            x u, l: each diagonal block's own, its largest entry
+//                             in [2^8, 2^9); the diagonal-block kernel writes them
+//                             and the result scales 1 / (s u) (L21) and 1 / (l s) (U12)
+// FP16 holds up to 65504, so a Z-sized operand may grow 2^7 past max |diag Z| and a
+// multiplier may reach 2^10 before it overflows; the lo part keeps 2^-25 of the
+// value or, below FP16's normal range, an absolute 2^-25.
+static const float kOrderOne = 64.f;
+
+namespace tc {
+// One CTA: s from the diagonal of A (n x n, lda).
+__global__ void __launch_bounds__(1024) k_lu_scale(const float2* __restrict__ A, int64_t lda, int n, float* sc) {
+    __shared__ float red[32];
+    float m = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float2 a = A[int64_t(i) * lda + i];
+        m = fmaxf(m, fmaxf(fabsf(a.x), fabsf(a.y)));   // fmaxf drops NaN
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) {
+            int ex = 0;   // s = 1 for a zero or non-finite diagonal
+            if (m > 0.f && isfinite(m)) {
+                const int eb = int((__float_as_uint(m) >> 23) & 0xFF);   // 0 for a subnormal maximum
+                ex = min(60, max(-60, 135 - max(eb, 1)));                 // 2^(eb-127) <= m < 2^(eb-126)
+            }
+            *sc = __uint_as_float(uint32_t(127 + ex) << 23);
+        }
+    }
+}
+}  // namespace tc
 
 int tc_diag_split_slots(frico_gpu_ctx* ctx, TcDiagSplit* out) {
     int rc;
@@ -635,7 +822,23 @@ int tc_diag_split_slots(frico_gpu_ctx* ctx, TcDiagSplit* out) {
     out->ul = s.ul;
     out->lh = s.lh;
     out->ll = s.ll;
+    out->h = panel_f16(ctx) ? 1 : 0;
+    out->sc = s.scale;
+    out->res_l21 = s.scale + 1;
+    out->res_u12 = s.scale + 2;
     return FRICO_GPU_OK;
+}
+
+// The operand scale s of the 3xFP16 block columns, from the diagonal of A (a
+// no-op for 3xTF32 operands); before the first diagonal block.
+int tc_lu_scale(frico_gpu_ctx* ctx, const float2* A, int64_t lda, int n) {
+    if (!panel_f16(ctx)) return FRICO_GPU_OK;
+    int rc;
+    if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
+    const PanelSlots s = panel_slots(ctx->tc_ws.p, ctx->n);
+    tc::k_lu_scale<<<1, 1024, 0, ctx->stream>>>(A, lda, n, s.scale);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_lu_scale");
 }
 
 // A21 (rest x 128, below the diagonal block) as A* and A12 (128 x rest, right of it)
@@ -646,10 +849,12 @@ int tc_lu_panel_split(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb
     int rc;
     if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
     const PanelSlots s = panel_slots(ctx->tc_ws.p, ctx->n);
+    const Pow2Scale zs{s.scale, 1.f, 1};
+    const Pow2Scale* h = panel_f16(ctx) ? &zs : nullptr;
     float2* A21 = A + int64_t(k0) * lda + k0 + jb;
     float2* A12 = A + int64_t(k0 + jb) * lda + k0;
-    const tc::SplitPart parts[2] = {split_part(false, A21, lda, rest, jb, s.a21h, s.a21l, KP),
-                                    split_part(true, A12, lda, rest, jb, s.a12h, s.a12l, KP)};
+    const tc::SplitPart parts[2] = {split_part(false, A21, lda, rest, jb, s.a21h, s.a21l, KP, h),
+                                    split_part(true, A12, lda, rest, jb, s.a12h, s.a12l, KP, h)};
     return launch_split(ctx, ctx->stream, parts, 2, KP);
 }
 
@@ -664,18 +869,27 @@ int tc_lu_panel(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int 
     int rc;
     if ((rc = ensure(ctx, ctx->tc_ws, tc_panel_ws_bytes(ctx->n)))) return rc;
     const PanelSlots s = panel_slots(ctx->tc_ws.p, ctx->n);
+    const bool h = panel_f16(ctx);
     out->Lah = s.lah;
     out->Lal = s.lal;
     out->Ubh = s.ubh;
     out->Ubl = s.ubl;
     out->rest = rest;
     out->KP = KP;
+    out->h = h ? 1 : 0;
+    out->sc = s.scale;
     float2* A21 = A + int64_t(k0) * lda + k0 + jb;
     float2* A12 = A + int64_t(k0 + jb) * lda + k0;
+    // L21: (A21 s)(U11^-1 u) = s u L21, emitted as 2^6 L21;
+    // U12: (L11^-1 l)(A12 s) = l s U12, emitted as s U12
+    const Pow2Scale r1{s.scale + 1, 1.f, 1}, e1{nullptr, kOrderOne, 0};
+    const Pow2Scale r2{s.scale + 2, 1.f, 1}, e2{s.scale, 1.f, 1};
     TcProblem q[2];
-    if ((rc = make_problem(ctx, q[0], A21, lda, 2 * rest, jb, s.a21h, s.a21l, s.uh, s.ul, KP, 0, 1, s.lah, s.lal)))
+    if ((rc = make_problem(ctx, q[0], A21, lda, 2 * rest, jb, s.a21h, s.a21l, s.uh, s.ul, KP, 0, 1, s.lah, s.lal,
+                           h ? &r1 : nullptr, h ? &e1 : nullptr)))
         return rc;
-    if ((rc = make_problem(ctx, q[1], A12, lda, 2 * jb, rest, s.lh, s.ll, s.a12h, s.a12l, KP, 0, 2, s.ubh, s.ubl)))
+    if ((rc = make_problem(ctx, q[1], A12, lda, 2 * jb, rest, s.lh, s.ll, s.a12h, s.a12l, KP, 0, 2, s.ubh, s.ubl,
+                           h ? &r2 : nullptr, h ? &e2 : nullptr)))
         return rc;
     return launch_gemm(ctx, ctx->stream, q, 2, KP, 0, nullptr);
 }
@@ -685,10 +899,13 @@ int tc_lu_update(frico_gpu_ctx* ctx, const TcPanel& pn, float2* C, int64_t ldc, 
                  cudaEvent_t* ev) {
     if (ncols <= 0) return FRICO_GPU_OK;
     const int KP = pn.KP;
+    const size_t esz = pn.h ? 2 : 4, boff_bytes = size_t(boff) * KP * esz;
+    // (L21 2^6)(U12 s) = 2^6 s L21 U12
+    const Pow2Scale r3{pn.sc, 1.f / kOrderOne, -1};
     TcProblem q;
     int rc;
-    if ((rc = make_problem(ctx, q, C, ldc, 2 * pn.rest, ncols, pn.Lah, pn.Lal, pn.Ubh + int64_t(boff) * KP,
-                           pn.Ubl + int64_t(boff) * KP, KP, 1, 0, nullptr, nullptr)))
+    if ((rc = make_problem(ctx, q, C, ldc, 2 * pn.rest, ncols, pn.Lah, pn.Lal, (const char*)pn.Ubh + boff_bytes,
+                           (const char*)pn.Ubl + boff_bytes, KP, 1, 0, nullptr, nullptr, pn.h ? &r3 : nullptr)))
         return rc;
     return launch_gemm(ctx, ctx->stream, &q, 1, KP, max_ctas, ev);
 }

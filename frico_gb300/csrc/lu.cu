@@ -751,7 +751,7 @@ template <typename R> struct LuDriver {
         trsm_smem = sizeof(C) * (kNB * kNB + 32 * kNB);
         const int eng = ctx->opt.gemm_engine;
         use_tc = sizeof(R) == 4 && eng != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
-        if (eng == FRICO_GEMM_TC && sizeof(R) == 4 && !use_tc)
+        if ((eng == FRICO_GEMM_TC || eng == FRICO_GEMM_TC_F16) && sizeof(R) == 4 && !use_tc)
             return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
         return cuda_check(ctx, cudaFuncSetAttribute(k_trsm_lower_unit<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     int(trsm_smem)), "trsm smem attribute");

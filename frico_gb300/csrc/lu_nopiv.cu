@@ -15,6 +15,7 @@
 //   k_trsm_right   L21 = A21 U11^{-1}, 64 rows per CTA
 //   k_trsm_lower_unit (lu.cu)   U12 = L11^{-1} A12
 //   trailing update A22 -= L21 U12 (tensor cores when available)
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,6 +52,7 @@ template <typename C> __device__ __forceinline__ bool cfinite(C a) { return isfi
 //      X[r][c] = T[r][c] / U[c][c] (r <= c),  T[r][j] -= X[r][c] U[c][j] (j > c),
 //    the same rank-1 form as the elimination of the rows below.
 static const int kDLD = kNP + 1;   // shared leading dimension (conflict-free tile reads)
+static const int kDiagThreads = 256;
 
 // Steps c = 16 P .. 16 P + 15. LOWER: the multipliers (L) go to S[c * kDLD + r], r > c.
 template <int P, bool LOWER, typename C>
@@ -141,28 +143,67 @@ template <typename C> constexpr size_t diag_lu_smem() { return sizeof(C) * (size
 // CTA 1 writes the LU to A and L^{-1}, CTA 0 U^{-1}; both read the block from
 // `src`, a copy made before the launch (ld 128), so CTA 1 may overwrite A
 // whatever the other's timing.
-// With usplit / lsplit (complex64 only): U^{-1} also as the hi/lo TF32 B^ operand
-// of L21 = A21 U^{-1} (row j = column j of U^{-1}, 256 floats: the hi/lo of the
+// With usplit / lsplit (complex64 only): U^{-1} also as the hi/lo B^ operand
+// of L21 = A21 U^{-1} (row j = column j of U^{-1}, 256 values: the hi/lo of the
 // column-major array itself), L^{-1} as the A* operand of U12 = L^{-1} A12
-// (rows 2r = (re, -im), 2r + 1 = (im, re) of row r, 256 floats each).
+// (rows 2r = (re, -im), 2r + 1 = (im, re) of row r, 256 values each); TF32 in
+// float pairs or (sp.h) FP16 in half pairs, each inverse scaled by the power of
+// two u (l) that puts its largest entry in [2^8, 2^9), with 1 / (s u) and
+// 1 / (l s) (s = *sp.sc) to sp.res_l21 and sp.res_u12 for the GEMMs' results.
 __device__ __forceinline__ float2 tf32_hi2(float2 v) {
     return make_float2(__uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u),
                        __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u));
 }
 
+// Largest |re|, |im| over the CTA (every thread of the CTA calls it; red: 32 floats).
+__device__ __forceinline__ float cta_absmax(float m, float* red) {
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = 0.f;
+    for (int w = 0; w < int(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
+    __syncthreads();
+    return m;
+}
+
+// The power of two that puts m in [2^8, 2^9) (1 for zero or non-finite m).
+__device__ __forceinline__ float pow2_for(float m) {
+    int ex = 0;
+    if (m > 0.f && isfinite(m)) {
+        const int eb = int((__float_as_uint(m) >> 23) & 0xFF);   // 2^(eb-127) <= m < 2^(eb-126)
+        ex = min(60, max(-60, 135 - max(eb, 1)));
+    }
+    return __uint_as_float(uint32_t(127 + ex) << 23);
+}
+
+// Pair a (already scaled for FP16) as hi/lo operands at pair index o.
+__device__ __forceinline__ void put_split2(void* hp, void* lp, int64_t o, float2 a, bool h) {
+    if (h) {
+        const __half2 hi = __floats2half2_rn(a.x, a.y);
+        const float2 hf = __half22float2(hi);
+        ((__half2*)hp)[o] = hi;
+        ((__half2*)lp)[o] = __floats2half2_rn(a.x - hf.x, a.y - hf.y);
+    } else {
+        const float2 hi = tf32_hi2(a);
+        ((float2*)hp)[o] = hi;
+        ((float2*)lp)[o] = make_float2(a.x - hi.x, a.y - hi.y);
+    }
+}
+
 template <typename C>
-__global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0, int jb,
-                                                C* Uinv, C* Linv, DeviceStatus* st, float2* usplit_h,
-                                                float2* usplit_l, float2* lsplit_h, float2* lsplit_l) {
+__global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0,
+                                                         int jb, C* Uinv, C* Linv, DeviceStatus* st,
+                                                         TcDiagSplit sp) {
     using R = decltype(A[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
     C* S = (C*)smraw;              // S[c * kDLD + r]
     C* vb = S + kNP * kDLD;        // 4 x kNP published rows / columns
+    __shared__ float red[32];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const bool lower = blockIdx.x == 1;
 #pragma unroll 16
-    for (int it = 0; it < kNP * kNP / 256; it++) {
-        const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+    for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {
+        const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
         S[c * kDLD + r] = (r < jb && c < jb) ? src[c * kNP + r] : cmake(R(r == c ? 1 : 0), R(0));
     }
     __syncthreads();
@@ -181,8 +222,8 @@ __global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A
                 if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
         __syncthreads();
 #pragma unroll 16
-        for (int it = 0; it < kNP * kNP / 256; it++) {
-            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {
+            const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
             if (r < jb && c < jb) A[int64_t(k0 + c) * lda + k0 + r] = S[c * kDLD + r];
         }
         __syncthreads();   // S takes L^{-1} (strict lower of W)
@@ -193,22 +234,33 @@ __global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A
                 if (ty + 16 * i > tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
         __syncthreads();
 #pragma unroll 8
-        for (int it = 0; it < kNP * kNP / 256; it++) {   // full 128 x 128, identity past jb
-            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {   // full 128 x 128, identity past jb
+            const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
             Linv[c * kNP + r] = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
         }
-        if (lsplit_h) {
+        if (sp.lh) {
+            const bool h = sp.h != 0;
+            float ls = 1.f;
+            if (h) {   // l from the largest entry of L^{-1} (unit diagonal included)
+                float m = 1.f;
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        if (ty + 16 * i > tx + 16 * j)
+                            m = fmaxf(m, fmaxf(fabsf(float(v[i][j].x)), fabsf(float(v[i][j].y))));
+                ls = pow2_for(cta_absmax(m, red));
+                if (threadIdx.x == 0) *sp.res_u12 = 1.f / (ls * *sp.sc);   // powers of two: exact
+            }
 #pragma unroll 4
-            for (int it = 0; it < kNP * kNP / 256; it++) {   // A* rows 2r, 2r + 1 at K = 2c, 2c + 1
-                const int idx = threadIdx.x + 256 * it, c = idx & (kNP - 1), r = idx >> 7;
+            for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {   // A* rows 2r, 2r + 1 at K = 2c, 2c + 1
+                const int idx = threadIdx.x + kDiagThreads * it, c = idx & (kNP - 1), r = idx >> 7;
                 const C v = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
-                const float2 a0 = make_float2(float(v.x), -float(v.y)), a1 = make_float2(float(v.y), float(v.x));
-                const float2 h0 = tf32_hi2(a0), h1 = tf32_hi2(a1);
-                const int64_t o0 = int64_t(2 * r) * kNP + c, o1 = o0 + kNP;   // float2 units, rows of 256 floats
-                lsplit_h[o0] = h0;
-                lsplit_h[o1] = h1;
-                lsplit_l[o0] = make_float2(a0.x - h0.x, a0.y - h0.y);
-                lsplit_l[o1] = make_float2(a1.x - h1.x, a1.y - h1.y);
+                const float2 a0 = make_float2(float(v.x) * ls, -float(v.y) * ls);
+                const float2 a1 = make_float2(float(v.y) * ls, float(v.x) * ls);
+                const int64_t o0 = int64_t(2 * r) * kNP + c, o1 = o0 + kNP;   // pair units, rows of 256 values
+                put_split2(sp.lh, sp.ll, o0, a0, h);
+                put_split2(sp.lh, sp.ll, o1, a1, h);
             }
         }
     } else {
@@ -220,16 +272,25 @@ __global__ void __launch_bounds__(256) k_diag_lu(const C* __restrict__ src, C* A
             for (int j = 0; j < 8; j++)
                 if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
         __syncthreads();
+        const bool h = sp.h != 0 && sp.uh;
+        float us = 1.f;
+        if (h) {   // u from the largest entry of U^{-1}
+            float m = 0.f;
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (ty + 16 * i <= tx + 16 * j)
+                        m = fmaxf(m, fmaxf(fabsf(float(v[i][j].x)), fabsf(float(v[i][j].y))));
+            us = pow2_for(cta_absmax(m, red));
+            if (threadIdx.x == 0) *sp.res_l21 = 1.f / (*sp.sc * us);   // powers of two: exact
+        }
 #pragma unroll 8
-        for (int it = 0; it < kNP * kNP / 256; it++) {
-            const int idx = threadIdx.x + 256 * it, r = idx & (kNP - 1), c = idx >> 7;
+        for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {
+            const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
             const C v = r <= c ? S[c * kDLD + r] : cmake(R(0), R(0));
             Uinv[c * kNP + r] = v;
-            if (usplit_h) {
-                const float2 a = make_float2(float(v.x), float(v.y)), h = tf32_hi2(a);
-                usplit_h[c * kNP + r] = h;
-                usplit_l[c * kNP + r] = make_float2(a.x - h.x, a.y - h.y);
-            }
+            if (sp.uh) put_split2(sp.uh, sp.ul, c * kNP + r, make_float2(float(v.x) * us, float(v.y) * us), h);
         }
     }
 }
@@ -387,9 +448,9 @@ template <typename C> __global__ void k_copy_block(const C* __restrict__ A, int6
 static int launch_diag_lu(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_t lda, int k0, int jb,
                           float2* Uinv, float2* Linv, float2* blk, DeviceStatus* dst, const TcDiagSplit* sp = nullptr) {
     k_copy_block<float2><<<16, 256, 0, st>>>(A, lda, k0, jb, blk);
-    k_diag_lu<float2><<<2, 256, diag_lu_smem<float2>(), st>>>(
-        blk, A, lda, k0, jb, Uinv, Linv, dst, sp ? (float2*)sp->uh : nullptr, sp ? (float2*)sp->ul : nullptr,
-        sp ? (float2*)sp->lh : nullptr, sp ? (float2*)sp->ll : nullptr);
+    TcDiagSplit none{};
+    k_diag_lu<float2><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv, dst,
+                                                                       sp ? *sp : none);
     count_launch(ctx, 2);
     return cuda_check(ctx, cudaGetLastError(), "k_diag_lu");
 }
@@ -411,11 +472,11 @@ static int launch_uinv_blocks(frico_gpu_ctx* ctx, cudaStream_t st, const float2*
 template <typename F> static int run_lu_graph(frico_gpu_ctx* ctx, F&& enqueue) {
     LuGraph& g = ctx->lu_graph;
     if (ctx->opt.profile_kernels) return enqueue();
-    const uintptr_t key[10] = {uintptr_t(ctx->n), uintptr_t(ctx->z32.p), uintptr_t(ctx->dinv128.p),
+    const uintptr_t key[11] = {uintptr_t(ctx->n), uintptr_t(ctx->z32.p), uintptr_t(ctx->dinv128.p),
                                uintptr_t(ctx->panel_ws.p), uintptr_t(ctx->tc_ws.p), uintptr_t(ctx->status.p),
                                uintptr_t(ctx->ipiv.p), uintptr_t(ctx->perm.p), uintptr_t(ctx->stream2),
-                               uintptr_t(ctx->tc_ws.bytes)};
-    const bool same = std::equal(key, key + 10, g.key);
+                               uintptr_t(ctx->tc_ws.bytes), uintptr_t(ctx->opt.gemm_engine)};
+    const bool same = std::equal(key, key + 11, g.key);
     cudaStream_t st = ctx->stream;
     if (same && g.exec) {
         ctx->stats.kernel_launches += g.launches;
@@ -427,7 +488,7 @@ template <typename F> static int run_lu_graph(frico_gpu_ctx* ctx, F&& enqueue) {
     if (!same) {   // first call with this key: run eagerly
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
-        std::copy(key, key + 10, g.key);
+        std::copy(key, key + 11, g.key);
         return enqueue();
     }
     const int64_t l0 = ctx->stats.kernel_launches;
@@ -499,7 +560,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
          })))
         return rc;
     const bool tc = ctx->opt.gemm_engine != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
-    if (ctx->opt.gemm_engine == FRICO_GEMM_TC && !tc)
+    if ((ctx->opt.gemm_engine == FRICO_GEMM_TC || ctx->opt.gemm_engine == FRICO_GEMM_TC_F16) && !tc)
         return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
     if (tc) {
         // every buffer the factorisation touches is sized before the first launch, so that
@@ -518,6 +579,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             cudaEvent_t ev_narrow = ctx->la_ev[0], ev_diag = ctx->la_ev[1];
             TcDiagSplit dsp;
             if ((rc = tc_diag_split_slots(ctx, &dsp))) return rc;
+            if ((rc = tc_lu_scale(ctx, A, lda, n))) return rc;   // operand scale of the 3xFP16 block columns
             if ((rc = launch_diag_lu(ctx, st, A, lda, 0, std::min(kNP, n), Uinv_of(0), Linv_of(0), Blk, dst, &dsp)))
                 return rc;
             if (n > kNP && (rc = tc_lu_panel_split(ctx, A, lda, 0, kNP, n - kNP))) return rc;

@@ -116,7 +116,8 @@ class Simulation:
                                 _abi.PREC_MIXED if precision == "mixed" else _abi.PREC_FP64,
                                 _abi.HPHASE_PHYSICAL if h_phase == "physical" else _abi.HPHASE_COMPAT,
                                 max_refine_iters, refine_tol, Z0, int(profile_kernels),
-                                {"auto": _abi.GEMM_AUTO, "simt": _abi.GEMM_SIMT, "tc": _abi.GEMM_TC}[gemm_engine],
+                                {"auto": _abi.GEMM_AUTO, "simt": _abi.GEMM_SIMT, "tc": _abi.GEMM_TC,
+                                 "tc_f16": _abi.GEMM_TC_F16}[gemm_engine],
                                 {"auto": _abi.PIVOT_AUTO, "partial": _abi.PIVOT_PARTIAL,
                                  "none": _abi.PIVOT_NONE}[pivoting],
                                 {"auto": _abi.REFINE_AUTO, "classic": _abi.REFINE_CLASSIC}[refine],

@@ -103,9 +103,11 @@ typedef struct frico_gpu_options {
 #define FRICO_PIVOT_PARTIAL 1  /* LAPACK zgetrf partial pivoting                        */
 #define FRICO_PIVOT_NONE    2  /* no interchanges (refinement failure is an error)      */
 
-#define FRICO_GEMM_AUTO 0   /* tcgen05 3xTF32 on sm_103, SIMT otherwise */
-#define FRICO_GEMM_SIMT 1   /* CUDA-core FP32 complex GEMM               */
-#define FRICO_GEMM_TC   2   /* tcgen05 3xTF32 (error if unavailable)     */
+#define FRICO_GEMM_AUTO   0  /* tcgen05 3xTF32 on sm_103, SIMT otherwise */
+#define FRICO_GEMM_SIMT   1  /* CUDA-core FP32 complex GEMM               */
+#define FRICO_GEMM_TC     2  /* tcgen05 3xTF32 (error if unavailable)     */
+#define FRICO_GEMM_TC_F16 3  /* tcgen05; the unpivoted LU's block columns with 3xFP16 operands
+                                scaled by powers of two, other updates 3xTF32 (error if unavailable) */
 
 typedef struct frico_c64 { float re, im; } frico_c64;
 
@@ -342,7 +344,8 @@ int frico_gpu_rcs_points(frico_gpu_ctx* ctx, int32_t col, double R, int64_t npts
 int frico_gpu_last_stats(frico_gpu_ctx* ctx, frico_gpu_stats* stats);
 
 /* Diagnostic: C -= A B with the LU's complex64 trailing-update kernel
- * (engine FRICO_GEMM_SIMT or FRICO_GEMM_TC); A m x k (ld m), B k x n (ld k),
+ * (engine FRICO_GEMM_SIMT, FRICO_GEMM_TC: 3xTF32 operands, or
+ * FRICO_GEMM_TC_F16: 3xFP16 operands); A m x k (ld m), B k x n (ld k),
  * C m x n (ld m), column-major host buffers. No FRICO counterpart: it exposes
  * one internal kernel so that it can be tested on its own. */
 int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, int32_t k, const frico_c64* A,

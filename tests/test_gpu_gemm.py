@@ -1,6 +1,7 @@
-"""The LU's complex64 trailing-update kernels (SIMT and tcgen05 3xTF32) on
-their own, through the diagnostic C-ABI entry point, against a complex128
-product. 3xTF32 keeps FP32-level accuracy: the tolerance is 2e-6 relative."""
+"""The LU's complex64 trailing-update kernels (SIMT, tcgen05 3xFP16 and
+3xTF32) on their own, through the diagnostic C-ABI entry point, against a
+complex128 product. The split products keep FP32-level accuracy (FP16 and TF32
+both carry 10 explicit mantissa bits): the tolerance is 2e-6 relative."""
 import ctypes as C
 
 import numpy as np
@@ -32,7 +33,7 @@ def ctx(gpu_lib):
 @pytest.mark.parametrize("m,n,k", [(128, 128, 64), (300, 200, 64), (1000, 700, 64), (257, 129, 50), (64, 300, 17),
                                    (1000, 700, 128), (777, 513, 128),
                                    (2048, 1536, 64)])
-@pytest.mark.parametrize("engine", ["simt", "tc"])
+@pytest.mark.parametrize("engine", ["simt", "tc", "tc_f16"])
 def test_cgemm(gpu_lib, ctx, m, n, k, engine):
     from frico_gb300 import _abi
     rng = np.random.default_rng(m * 7 + n * 3 + k)
@@ -40,7 +41,8 @@ def test_cgemm(gpu_lib, ctx, m, n, k, engine):
     B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))).astype(np.complex64)
     C0 = (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))).astype(np.complex64)
     ref = C0.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
-    out = run(gpu_lib, ctx, A, B, C0, _abi.GEMM_TC if engine == "tc" else _abi.GEMM_SIMT)
+    eng = {"simt": _abi.GEMM_SIMT, "tc": _abi.GEMM_TC, "tc_f16": _abi.GEMM_TC_F16}[engine]
+    out = run(gpu_lib, ctx, A, B, C0, eng)
     err = np.abs(out - ref).max() / np.abs(ref).max()
     # FP32 accumulation (both engines): rounding grows with the K terms summed
     assert err < 2e-6 * max(1.0, k / 64) ** 0.75, err

@@ -151,7 +151,7 @@ def test_mixed_precision_sphere(gpu_lib):
 
 
 @pytest.mark.parametrize("pivoting,engine", [("auto", "auto"), ("none", "simt"), ("partial", "auto"),
-                                             ("partial", "simt")])
+                                             ("partial", "simt"), ("auto", "tc_f16")])
 def test_mixed_pivoting_modes(gpu_lib, pivoting, engine):
     """Every complex64 factorisation strategy refines to the FP64 solution."""
     m = meshes.icosphere(3)
