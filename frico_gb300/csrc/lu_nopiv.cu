@@ -190,7 +190,7 @@ __device__ __forceinline__ void put_split2(void* hp, void* lp, int64_t o, float2
     }
 }
 
-template <typename C>
+template <typename C, bool F16>
 __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0,
                                                          int jb, C* Uinv, C* Linv, DeviceStatus* st,
                                                          TcDiagSplit sp) {
@@ -198,7 +198,6 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
     extern __shared__ __align__(16) unsigned char smraw[];
     C* S = (C*)smraw;              // S[c * kDLD + r]
     C* vb = S + kNP * kDLD;        // 4 x kNP published rows / columns
-    __shared__ float red[32];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const bool lower = blockIdx.x == 1;
 #pragma unroll 16
@@ -239,9 +238,9 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
             Linv[c * kNP + r] = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
         }
         if (sp.lh) {
-            const bool h = sp.h != 0;
             float ls = 1.f;
-            if (h) {   // l from the largest entry of L^{-1} (unit diagonal included)
+            if constexpr (F16) {   // l from the largest entry of L^{-1} (unit diagonal included)
+                __shared__ float red[32];
                 float m = 1.f;
 #pragma unroll
                 for (int i = 0; i < 8; i++)
@@ -256,11 +255,14 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
             for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {   // A* rows 2r, 2r + 1 at K = 2c, 2c + 1
                 const int idx = threadIdx.x + kDiagThreads * it, c = idx & (kNP - 1), r = idx >> 7;
                 const C v = r > c ? S[c * kDLD + r] : cmake(R(r == c ? 1 : 0), R(0));
-                const float2 a0 = make_float2(float(v.x) * ls, -float(v.y) * ls);
-                const float2 a1 = make_float2(float(v.y) * ls, float(v.x) * ls);
+                float2 a0 = make_float2(float(v.x), -float(v.y)), a1 = make_float2(float(v.y), float(v.x));
+                if constexpr (F16) {
+                    a0 = make_float2(a0.x * ls, a0.y * ls);
+                    a1 = make_float2(a1.x * ls, a1.y * ls);
+                }
                 const int64_t o0 = int64_t(2 * r) * kNP + c, o1 = o0 + kNP;   // pair units, rows of 256 values
-                put_split2(sp.lh, sp.ll, o0, a0, h);
-                put_split2(sp.lh, sp.ll, o1, a1, h);
+                put_split2(sp.lh, sp.ll, o0, a0, F16);
+                put_split2(sp.lh, sp.ll, o1, a1, F16);
             }
         }
     } else {
@@ -272,9 +274,9 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
             for (int j = 0; j < 8; j++)
                 if (ty + 16 * i <= tx + 16 * j) S[(tx + 16 * j) * kDLD + ty + 16 * i] = v[i][j];
         __syncthreads();
-        const bool h = sp.h != 0 && sp.uh;
         float us = 1.f;
-        if (h) {   // u from the largest entry of U^{-1}
+        if constexpr (F16) {   // u from the largest entry of U^{-1}
+            __shared__ float red[32];
             float m = 0.f;
 #pragma unroll
             for (int i = 0; i < 8; i++)
@@ -290,7 +292,11 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
             const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
             const C v = r <= c ? S[c * kDLD + r] : cmake(R(0), R(0));
             Uinv[c * kNP + r] = v;
-            if (sp.uh) put_split2(sp.uh, sp.ul, c * kNP + r, make_float2(float(v.x) * us, float(v.y) * us), h);
+            if (sp.uh) {
+                float2 a = make_float2(float(v.x), float(v.y));
+                if constexpr (F16) a = make_float2(a.x * us, a.y * us);
+                put_split2(sp.uh, sp.ul, c * kNP + r, a, F16);
+            }
         }
     }
 }
@@ -449,8 +455,12 @@ static int launch_diag_lu(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_
                           float2* Uinv, float2* Linv, float2* blk, DeviceStatus* dst, const TcDiagSplit* sp = nullptr) {
     k_copy_block<float2><<<16, 256, 0, st>>>(A, lda, k0, jb, blk);
     TcDiagSplit none{};
-    k_diag_lu<float2><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv, dst,
-                                                                       sp ? *sp : none);
+    if (sp && sp->h)
+        k_diag_lu<float2, true><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv,
+                                                                                 dst, *sp);
+    else
+        k_diag_lu<float2, false><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv,
+                                                                                  dst, sp ? *sp : none);
     count_launch(ctx, 2);
     return cuda_check(ctx, cudaGetLastError(), "k_diag_lu");
 }
@@ -547,8 +557,12 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     auto Linv_of = [&](int k0) { return (C*)ctx->dinv128.p + size_t(k0 / kNP) * kNP * kNP; };
     auto Uinv_of = [&](int k0) { return (C*)ctx->dinv128.p + size_t(nbk + k0 / kNP) * kNP * kNP; };
     if ((rc = device_once(ctx, kOnceNopivLu, [](frico_gpu_ctx* c) {
-             int r = cuda_check(c, cudaFuncSetAttribute(k_diag_lu<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+             int r = cuda_check(c, cudaFuncSetAttribute(k_diag_lu<float2, false>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         int(diag_lu_smem<float2>())), "diag smem");
+             if (r) return r;
+             r = cuda_check(c, cudaFuncSetAttribute(k_diag_lu<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    int(diag_lu_smem<float2>())), "diag smem");
              if (r) return r;
              r = cuda_check(c, cudaFuncSetAttribute(k_uinv_blocks<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     int(uinv_smem<float2>())), "uinv smem");
