@@ -135,14 +135,17 @@ __device__ __forceinline__ void diag_sweep(C (&v)[8][8], C* S, C* vb, int tx, in
 
 template <typename C> constexpr size_t diag_lu_smem() { return sizeof(C) * (size_t(kNP) * kDLD + 4 * kNP); }
 
-// LU (no interchanges) of the jb x jb diagonal block at (k0, k0), written back
-// in place; U11^{-1} to Uinv and L11^{-1} (unit lower) to Linv, both 128 x 128
+// LU (no interchanges) of the jb x jb diagonal block at (k0, k0) of the
+// matrix, read from src (leading dimension lds) and written to dlu (ldd);
+// U11^{-1} to Uinv and L11^{-1} (unit lower) to Linv, both 128 x 128
 // column-major (the GEMMs read their jb x jb part with leading dimension 128,
 // the chained solves the whole block). A block narrower than 128 is padded
 // with the identity. A zero or non-finite pivot sets st->info (first one).
-// CTA 1 writes the LU to A and L^{-1}, CTA 0 U^{-1}; both read the block from
-// `src`, a copy made before the launch (ld 128), so CTA 1 may overwrite A
-// whatever the other's timing.
+// CTA 1 writes the LU and L^{-1}, CTA 0 U^{-1}; both read src, so dlu must not
+// alias it: either src is a copy of the block (the SIMT path, dlu = the block
+// in A) or src is the block in A and dlu a staging slot that k_uinv_blocks
+// copies into A after the factorisation (the tensor-core path, whose later
+// steps never read the diagonal blocks of A).
 // With usplit / lsplit (complex64 only): U^{-1} also as the hi/lo B^ operand
 // of L21 = A21 U^{-1} (row j = column j of U^{-1}, 256 values: the hi/lo of the
 // column-major array itself), L^{-1} as the A* operand of U12 = L^{-1} A12
@@ -191,10 +194,10 @@ __device__ __forceinline__ void put_split2(void* hp, void* lp, int64_t o, float2
 }
 
 template <typename C, bool F16>
-__global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ src, C* A, int64_t lda, int k0,
-                                                         int jb, C* Uinv, C* Linv, DeviceStatus* st,
-                                                         TcDiagSplit sp) {
-    using R = decltype(A[0].x);
+__global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ src, int64_t lds, C* dlu,
+                                                         int64_t ldd, int k0, int jb, C* Uinv, C* Linv,
+                                                         DeviceStatus* st, TcDiagSplit sp) {
+    using R = decltype(src[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
     C* S = (C*)smraw;              // S[c * kDLD + r]
     C* vb = S + kNP * kDLD;        // 4 x kNP published rows / columns
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
 #pragma unroll 16
     for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {
         const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
-        S[c * kDLD + r] = (r < jb && c < jb) ? src[c * kNP + r] : cmake(R(r == c ? 1 : 0), R(0));
+        S[c * kDLD + r] = (r < jb && c < jb) ? src[c * lds + r] : cmake(R(r == c ? 1 : 0), R(0));
     }
     __syncthreads();
     C v[8][8];
@@ -223,7 +226,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_lu(const C* __restrict__ 
 #pragma unroll 16
         for (int it = 0; it < kNP * kNP / kDiagThreads; it++) {
             const int idx = threadIdx.x + kDiagThreads * it, r = idx & (kNP - 1), c = idx >> 7;
-            if (r < jb && c < jb) A[int64_t(k0 + c) * lda + k0 + r] = S[c * kDLD + r];
+            if (r < jb && c < jb) dlu[c * ldd + r] = S[c * kDLD + r];
         }
         __syncthreads();   // S takes L^{-1} (strict lower of W)
 #pragma unroll
@@ -342,10 +345,13 @@ __device__ __forceinline__ void uinv_phase(C (&x)[8][8], const C* S, C* vb, cons
 
 template <typename C> constexpr size_t uinv_smem() { return sizeof(C) * (size_t(kNP) * kDLD + 3 * kNP); }
 
-// Block b = blockIdx.x: U of the diagonal block at (128 b, 128 b) of A (identity
-// past n), its inverse to Uinv + b 128^2 (128 x 128 column-major).
+// Block b = blockIdx.x: U of the diagonal block at (128 b, 128 b) (identity past
+// n), its inverse to Uinv + b 128^2 (128 x 128 column-major). The block's LU is
+// read from A (stage == nullptr) or from the staging slot stage + b 128^2
+// (ld 128), which is then also copied into A.
 template <typename C>
-__global__ void __launch_bounds__(256) k_uinv_blocks(const C* __restrict__ A, int64_t lda, int n, C* Uinv) {
+__global__ void __launch_bounds__(256) k_uinv_blocks(C* A, int64_t lda, int n, const C* __restrict__ stage,
+                                                     C* Uinv) {
     using R = decltype(A[0].x);
     extern __shared__ __align__(16) unsigned char smraw[];
     C* S = (C*)smraw;              // S[c * kDLD + r]
@@ -353,10 +359,16 @@ __global__ void __launch_bounds__(256) k_uinv_blocks(const C* __restrict__ A, in
     C* rdiag = vb + 2 * kNP;
     const int k0 = blockIdx.x * kNP, jb = min(kNP, n - k0);
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const C* blk = stage ? stage + size_t(blockIdx.x) * kNP * kNP : A + int64_t(k0) * lda + k0;
+    const int64_t ldb = stage ? kNP : lda;
     for (int idx = threadIdx.x; idx < kNP * kNP; idx += 256) {
         const int r = idx & (kNP - 1), c = idx >> 7;
         C a = cmake(R(r == c ? 1 : 0), R(0));
-        if (r < jb && c < jb) a = r <= c ? A[int64_t(k0 + c) * lda + k0 + r] : cmake(R(0), R(0));
+        if (r < jb && c < jb) {
+            const C lu = blk[c * ldb + r];
+            if (stage) A[int64_t(k0 + c) * lda + k0 + r] = lu;
+            a = r <= c ? lu : cmake(R(0), R(0));
+        }
         S[c * kDLD + r] = a;
     }
     __syncthreads();
@@ -450,25 +462,42 @@ template <typename C> __global__ void k_copy_block(const C* __restrict__ A, int6
     }
 }
 
-// Copy of the diagonal block, then the two-CTA factor + inverses.
+// The two-CTA factor + inverses of the diagonal block at k0. With stage, the
+// kernel reads the block from A and writes its LU to stage (ld 128; copied into
+// A by k_uinv_blocks); without, the block is first copied to blk and its LU
+// written back into A.
 static int launch_diag_lu(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_t lda, int k0, int jb,
-                          float2* Uinv, float2* Linv, float2* blk, DeviceStatus* dst, const TcDiagSplit* sp = nullptr) {
-    k_copy_block<float2><<<16, 256, 0, st>>>(A, lda, k0, jb, blk);
+                          float2* Uinv, float2* Linv, float2* blk, float2* stage, DeviceStatus* dst,
+                          const TcDiagSplit* sp = nullptr) {
+    float2* Akk = A + int64_t(k0) * lda + k0;
+    const float2* src = Akk;
+    int64_t lds = lda, ldd = lda;
+    float2* dlu = Akk;
+    if (stage) {
+        dlu = stage;
+        ldd = kNP;
+    } else {
+        k_copy_block<float2><<<16, 256, 0, st>>>(A, lda, k0, jb, blk);
+        count_launch(ctx);
+        src = blk;
+        lds = kNP;
+    }
     TcDiagSplit none{};
     if (sp && sp->h)
-        k_diag_lu<float2, true><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv,
-                                                                                 dst, *sp);
+        k_diag_lu<float2, true><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(src, lds, dlu, ldd, k0, jb, Uinv,
+                                                                                 Linv, dst, *sp);
     else
-        k_diag_lu<float2, false><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(blk, A, lda, k0, jb, Uinv, Linv,
-                                                                                  dst, sp ? *sp : none);
-    count_launch(ctx, 2);
+        k_diag_lu<float2, false><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(src, lds, dlu, ldd, k0, jb, Uinv,
+                                                                                  Linv, dst, sp ? *sp : none);
+    count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_diag_lu");
 }
 
-// U^{-1} of all diagonal blocks for the chained solves (replacing the sweep's).
-static int launch_uinv_blocks(frico_gpu_ctx* ctx, cudaStream_t st, const float2* A, int64_t lda, int n,
-                              float2* Uinv0) {
-    k_uinv_blocks<float2><<<(n + kNP - 1) / kNP, 256, uinv_smem<float2>(), st>>>(A, lda, n, Uinv0);
+// U^{-1} of all diagonal blocks for the chained solves (replacing the sweep's);
+// with stage, the staged LU blocks are copied into A on the way.
+static int launch_uinv_blocks(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_t lda, int n,
+                              const float2* stage, float2* Uinv0) {
+    k_uinv_blocks<float2><<<(n + kNP - 1) / kNP, 256, uinv_smem<float2>(), st>>>(A, lda, n, stage, Uinv0);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_uinv_blocks");
 }
@@ -548,11 +577,14 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
     if ((rc = ensure(ctx, ctx->perm, sizeof(int32_t) * n))) return rc;
     if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
     const int nbk = (n + kNP - 1) / kNP;
-    if ((rc = ensure(ctx, ctx->panel_ws, sizeof(C) * kNP * kNP + 256))) return rc;
+    const bool tc = ctx->opt.gemm_engine != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
+    // tensor cores: one staging slot per diagonal block's LU; SIMT: one copy of the block being factored
+    if ((rc = ensure(ctx, ctx->panel_ws, sizeof(C) * (tc ? size_t(nbk) : 1) * kNP * kNP + 256))) return rc;
     if ((rc = ensure(ctx, ctx->dinv128, sizeof(C) * 4 * size_t(nbk) * kNP * kNP))) return rc;
     ctx->dinv128_valid = false;
     DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
-    C* Blk = (C*)ctx->panel_ws.p;   // copy of the diagonal block being factored
+    C* Blk = (C*)ctx->panel_ws.p;   // copy of the diagonal block being factored (SIMT) or the staging slots
+    auto stage_of = [&](int k0) { return Blk + size_t(k0 / kNP) * kNP * kNP; };
     // inverted diagonal blocks, kept for the chained solves: L^-1 of block b, U^-1 of block b
     auto Linv_of = [&](int k0) { return (C*)ctx->dinv128.p + size_t(k0 / kNP) * kNP * kNP; };
     auto Uinv_of = [&](int k0) { return (C*)ctx->dinv128.p + size_t(nbk + k0 / kNP) * kNP * kNP; };
@@ -573,7 +605,6 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                                "trsm_right smem");
          })))
         return rc;
-    const bool tc = ctx->opt.gemm_engine != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
     if ((ctx->opt.gemm_engine == FRICO_GEMM_TC || ctx->opt.gemm_engine == FRICO_GEMM_TC_F16) && !tc)
         return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
     if (tc) {
@@ -594,7 +625,8 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             TcDiagSplit dsp;
             if ((rc = tc_diag_split_slots(ctx, &dsp))) return rc;
             if ((rc = tc_lu_scale(ctx, A, lda, n))) return rc;   // operand scale of the 3xFP16 block columns
-            if ((rc = launch_diag_lu(ctx, st, A, lda, 0, std::min(kNP, n), Uinv_of(0), Linv_of(0), Blk, dst, &dsp)))
+            if ((rc = launch_diag_lu(ctx, st, A, lda, 0, std::min(kNP, n), Uinv_of(0), Linv_of(0), nullptr,
+                                     stage_of(0), dst, &dsp)))
                 return rc;
             if (n > kNP && (rc = tc_lu_panel_split(ctx, A, lda, 0, kNP, n - kNP))) return rc;
             bool diag_on_s2 = false;
@@ -620,8 +652,8 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                 if ((rc = tc_lu_update(ctx, pn, Cm, lda, 0, jb1, 0, ev))) return rc;
                 if ((rc = cuda_check(ctx, cudaEventRecord(ev_narrow, st), "record"))) return rc;
                 if ((rc = cuda_check(ctx, cudaStreamWaitEvent(s2, ev_narrow, 0), "wait narrow"))) return rc;
-                if ((rc = launch_diag_lu(ctx, s2, A, lda, k0 + jb, jb1, Uinv_of(k0 + jb), Linv_of(k0 + jb), Blk, dst,
-                                         &dsp)))
+                if ((rc = launch_diag_lu(ctx, s2, A, lda, k0 + jb, jb1, Uinv_of(k0 + jb), Linv_of(k0 + jb), nullptr,
+                                         stage_of(k0 + jb), dst, &dsp)))
                     return rc;
                 if ((rc = cuda_check(ctx, cudaEventRecord(ev_diag, s2), "record"))) return rc;
                 diag_on_s2 = true;
@@ -640,7 +672,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
                 }
                 if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
             }
-            if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0)))) return rc;
+            if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, Blk, Uinv_of(0)))) return rc;
             return trsv128_prepare(ctx, st);
         };
         if ((rc = run_lu_graph(ctx, enqueue))) return rc;
@@ -651,7 +683,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
         count_launch(ctx);
         for (int k0 = 0; k0 < n; k0 += kNP) {
             const int jb = std::min(kNP, n - k0);
-            if ((rc = launch_diag_lu(ctx, st, A, lda, k0, jb, Uinv_of(k0), Linv_of(k0), Blk, dst))) return rc;
+            if ((rc = launch_diag_lu(ctx, st, A, lda, k0, jb, Uinv_of(k0), Linv_of(k0), Blk, nullptr, dst))) return rc;
             const int rest = n - k0 - jb;
             if (rest > 0) {
                 // SIMT engine: L21 = A21 U11^{-1} with the inverse, U12 by the unit-lower TRSM
@@ -673,7 +705,7 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
             }
             if ((rc = cuda_check(ctx, cudaGetLastError(), "nopiv lu step"))) return rc;
         }
-        if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, Uinv_of(0)))) return rc;
+        if ((rc = launch_uinv_blocks(ctx, st, A, lda, n, nullptr, Uinv_of(0)))) return rc;
         if ((rc = trsv128_prepare(ctx, st))) return rc;
     }
     prof_event_collect(ctx);
