@@ -143,7 +143,7 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     DevBuf* bufs[] = {&ctx->xyz,     &ctx->tri,      &ctx->trigeo,   &ctx->qp,        &ctx->qps,     &ctx->rwg_itm,
                       &ctx->rwg_itp, &ctx->rwg_len,  &ctx->rwg_am,   &ctx->rwg_ap,    &ctx->rwg_vm,  &ctx->rwg_vp,
-                      &ctx->rwg_itf, &ctx->tri_bf,   &ctx->gtab,     &ctx->smom,      &ctx->basis_aux, &ctx->z64,
+                      &ctx->rwg_itf, &ctx->tri_bf,   &ctx->tri_new,  &ctx->tri_old,   &ctx->gtab,     &ctx->smom,      &ctx->basis_aux, &ctx->z64,
                       &ctx->z32,     &ctx->lu,       &ctx->ipiv,     &ctx->perm,      &ctx->panel_ws, &ctx->status,
                       &ctx->rhs,     &ctx->sol,      &ctx->rwork,    &ctx->rwork32,   &ctx->dwork32, &ctx->norms,
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
@@ -224,6 +224,19 @@ extern "C" int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* 
             tri_bf[3 * t + fill_cnt[t]++] = side ? int32_t(i + 1) : -int32_t(i + 1);
         }
     }
+    std::vector<int32_t> tri_new(nt, -1), tri_old(nt);
+    int32_t next = 0;
+    for (int64_t i = 0; i < n; i++)
+        for (const int32_t t : {itm[i], itp[i]})
+            if (tri_new[t] < 0) {
+                tri_new[t] = next;
+                tri_old[next++] = t;
+            }
+    for (int64_t t = 0; t < nt; t++)   // triangles without an RWG edge
+        if (tri_new[t] < 0) {
+            tri_new[t] = next;
+            tri_old[next++] = int32_t(t);
+        }
     int rc;
     auto up = [&](DevBuf& b, const void* src, size_t bytes) -> int {
         int r = ensure(ctx, b, bytes);
@@ -241,6 +254,8 @@ extern "C" int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* 
     if ((rc = up(ctx->rwg_vm, vm.data(), sizeof(double) * 3 * n))) return rc;
     if ((rc = up(ctx->rwg_vp, vp.data(), sizeof(double) * 3 * n))) return rc;
     if ((rc = up(ctx->tri_bf, tri_bf.data(), sizeof(int32_t) * 3 * nt))) return rc;
+    if ((rc = up(ctx->tri_new, tri_new.data(), sizeof(int32_t) * nt))) return rc;
+    if ((rc = up(ctx->tri_old, tri_old.data(), sizeof(int32_t) * nt))) return rc;
     ctx->nv = nv;
     ctx->nt = nt;
     ctx->n = n;

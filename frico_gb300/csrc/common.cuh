@@ -169,6 +169,11 @@ struct frico_gpu_ctx {
     frico::DevBuf xyz, tri, trigeo, qp, qps, rwg_itm, rwg_itp, rwg_len, rwg_am, rwg_ap, rwg_vm,
         rwg_vp, rwg_itf;
     frico::DevBuf tri_bf;         // [nt*3] basis index (+1, signed by side) per triangle slot
+    // triangles renumbered in order of first use by the RWGs (itm, then itp, in matrix order):
+    // the double-float Green table is indexed by these numbers, so the table entries of a tile
+    // of RWG pairs lie in a small block of it
+    frico::DevBuf tri_new;        // [nt] new number of each triangle
+    frico::DevBuf tri_old;        // [nt] triangle of each new number
     std::vector<frico_rwg> h_rwg; // host copy (port values, interfaces)
     std::vector<double> h_xyz;    // host copies of the mesh (sweep lanes are built from them)
     std::vector<int64_t> h_tri;

@@ -151,9 +151,11 @@ struct BasisDF {
     int32_t bad;
 };
 
+// dfo's triangle numbers are tnew's (the double-float table's) when tnew is given.
 __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo,
                             const double* __restrict__ qp, int nq, int mode, double inv_ksq,
-                            BasisAsm* __restrict__ out, BasisDF* __restrict__ dfo) {
+                            BasisAsm* __restrict__ out, BasisDF* __restrict__ dfo,
+                            const int32_t* __restrict__ tnew) {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= n) return;
     BasisAsm b;
@@ -191,8 +193,8 @@ __global__ void k_basis_aux(int64_t n, RwgDev rw, const TriGeo* __restrict__ geo
     out[i] = b;
     BasisDF f;
     int bad = 0;
-    f.itm = b.itm;
-    f.itp = b.itp;
+    f.itm = tnew ? tnew[b.itm] : b.itm;
+    f.itp = tnew ? tnew[b.itp] : b.itp;
     for (int d = 0; d < 3; d++) {
         split_df(b.u_m[d], f.um[d][0], f.um[d][1], bad);
         split_df(b.u_p[d], f.up[d][0], f.up[d][1], bad);
@@ -318,7 +320,9 @@ __global__ void __launch_bounds__(256) k_gtab_sym(int64_t nt, const QPoint* __re
 // sincos(kR) in double-float (dfloat.cuh); stored as (re hi, re lo, im hi,
 // im lo). A pair outside the double-float range (kR >= 6400, r^2 beyond the
 // split's exponents) is evaluated in FP64 and then split.
-__global__ void __launch_bounds__(256) k_gtab_sym_df(int64_t nt, const QPoint* __restrict__ qp, double k,
+// Table over the renumbered triangles: entry (a, b) is the pair (told[a], told[b]).
+__global__ void __launch_bounds__(256) k_gtab_sym_df(int64_t nt, const QPoint* __restrict__ qp,
+                                                    const int32_t* __restrict__ told, double k,
                                                     float4* __restrict__ G) {
     __shared__ double pa[32][3], pb[32][3];
     __shared__ float4 tile[32][33];
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(256) k_gtab_sym_df(int64_t nt, const QPoint* _
         int64_t t = (which ? tb : ta) * 32 + q;
         double* dst = which ? pb[q] : pa[q];
         if (t < nt) {
-            QPoint p = qp[t];
+            QPoint p = qp[told[t]];
             dst[0] = p.x; dst[1] = p.y; dst[2] = p.z;
         } else {
             dst[0] = dst[1] = dst[2] = 0.0;
@@ -447,6 +451,7 @@ struct AsmArgs {
     const BasisDF* bdf;  // the same, double-float (mode 0)
     const double2* G;    // mode 0/2: [nt*nt]; mode 1: 8 planes
     const float4* G4;    // mode 0, mixed: the table in double-float (re hi, re lo, im hi, im lo), else null
+    const int32_t* tnew; // with G4: G4's number of each triangle (BasisDF holds these numbers)
     const double2* S;    // split moments [n*4*8]
     double2* Z64;        // may be null
     float2* Z32;         // may be null
@@ -567,7 +572,7 @@ __device__ __forceinline__ double2 entry_mode0(const AsmArgs& A, const BasisAsm&
                                                                                    (t ? bj.hs_p : bj.hs_m))));
             double2 g;
             if (A.G4) {
-                const float4 q = A.G4[int64_t(ta) * A.nt + tb];
+                const float4 q = A.G4[int64_t(A.tnew[ta]) * A.nt + A.tnew[tb]];
                 g = make_double2(df_to_double(dmk(q.x, q.y)), df_to_double(dmk(q.z, q.w)));
             } else {
                 g = A.G[int64_t(ta) * A.nt + tb];
@@ -759,17 +764,19 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only) {
     const double* qp = (const double*)ctx->qp.p;
     const double* qps = (const double*)ctx->qps.p;
     cudaStream_t st = ctx->stream;
+    // double-float table and entries for the mixed path only: the FP64 drop-in (and the FP64
+    // factorisation a mixed solve falls back to) keep FP64 arithmetic throughout
+    const bool df = mode == 0 && ctx->opt.precision == FRICO_PREC_MIXED && !fp64_only;
+    const int32_t* tnew = (const int32_t*)ctx->tri_new.p;
     k_basis_aux<<<unsigned((n + 127) / 128), 128, 0, st>>>(n, rw, geo, qp, nq, mode, inv_ksq,
-                                                           (BasisAsm*)ctx->basis_aux.p, bdf);
+                                                           (BasisAsm*)ctx->basis_aux.p, bdf, df ? tnew : nullptr);
     dim3 gt(unsigned((nt + 127) / 128), unsigned(nt));
     double2* G = (double2*)ctx->gtab.p;
     const int64_t T = (nt + 31) / 32;
     const unsigned sym_blocks = unsigned(T * (T + 1) / 2);
-    // double-float table and entries for the mixed path only: the FP64 drop-in (and the FP64
-    // factorisation a mixed solve falls back to) keep FP64 arithmetic throughout
-    const bool df = mode == 0 && ctx->opt.precision == FRICO_PREC_MIXED && !fp64_only;
     if (df) {
-        k_gtab_sym_df<<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, k, (float4*)G);
+        k_gtab_sym_df<<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, (const int32_t*)ctx->tri_old.p, k,
+                                                  (float4*)G);
     } else if (mode == 0) {
         k_gtab_sym<0><<<sym_blocks, 256, 0, st>>>(nt, (const QPoint*)qp, geo, k, G);
     } else if (mode == 1) {
@@ -788,6 +795,7 @@ int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only) {
     a.bas = (const BasisAsm*)ctx->basis_aux.p;
     a.bdf = df ? bdf : nullptr;
     a.G4 = df ? (const float4*)G : nullptr;
+    a.tnew = df ? tnew : nullptr;
     ctx->z_df = df;
     a.G = G;
     a.S = (const double2*)ctx->smom.p;
