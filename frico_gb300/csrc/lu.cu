@@ -753,8 +753,11 @@ template <typename R> struct LuDriver {
         use_tc = sizeof(R) == 4 && eng != FRICO_GEMM_SIMT && gemm_tc_available(ctx);
         if ((eng == FRICO_GEMM_TC || eng == FRICO_GEMM_TC_F16) && sizeof(R) == 4 && !use_tc)
             return set_err(ctx, FRICO_GPU_EINVAL, "tensor-core GEMM engine not available on this device");
+        // never below what the unpivoted complex64 path needs (128-wide blocks, trsm_lower_unit_f32):
+        // the attribute belongs to the kernel on this device, not to this factorisation
+        const size_t attr = sizeof(R) == 4 ? std::max(trsm_smem, sizeof(C) * (128 * 128 + 32 * 128)) : trsm_smem;
         return cuda_check(ctx, cudaFuncSetAttribute(k_trsm_lower_unit<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    int(trsm_smem)), "trsm smem attribute");
+                                                    int(attr)), "trsm smem attribute");
     }
 
     // Widest leaf (<= w, power of two >= 8) the cluster kernel can hold for m rows; 0 if none.

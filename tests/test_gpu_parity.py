@@ -287,6 +287,33 @@ def test_multi_rhs_and_factors(gpu_lib, sphere2):
     assert rel_norm(L @ U, PA) < 1e-12
 
 
+@pytest.mark.parametrize("level", [2, 3])
+@pytest.mark.parametrize("engine", ["auto", "simt", "tc_f16"])
+def test_mixed_unpivoted_factors(gpu_lib, level, engine):
+    """The complex64 factors of the mixed path (no interchanges) reproduce Z:
+    every diagonal block's LU is in place after the factorisation, whether the
+    tensor-core path staged it (copied into A at the end) or the SIMT path
+    wrote it directly; N = 480 ends in a 96-row block, N = 1920 in whole ones."""
+    m = meshes.icosphere(level)
+    f = 450e6
+    Zr = oracle_for(m).compute_matrix(f)
+    sim = Simulation(m, precision="mixed", pivoting="none", gemm_engine=engine)
+    sim.compute_matrix(f)
+    sim.set_nrhs(1)
+    sim.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+    sim.solve()
+    assert sim.stats()["pivoting_used"] == 2
+    LU, ipiv = sim.get_factors()
+    n = Zr.shape[0]
+    np.testing.assert_array_equal(ipiv, np.arange(1, n + 1))
+    L = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    # complex64 factors: FP32 rounding times the growth; the 3xFP16 updates lose the lo parts of
+    # small entries (below FP16's normal range), so their factors are looser. A block left out
+    # of A would give an error of order one.
+    assert rel_norm(L @ U, Zr) < (1e-2 if engine == "tc_f16" else 1e-4)   # measured 1.2e-5 (tensor cores)
+
+
 def test_singular_matrix_info(gpu_lib):
     """The xy-hypot edge length makes vertical edges zero-length: Z gets zero
     rows/columns and zgetrf reports the first zero pivot; so must the GPU."""
