@@ -16,10 +16,14 @@ tagged by surface, and tagged 1-D curve segments (the delta-gap feed).
                  60 deg, joined by a 5 mm feed column of collinear edges
                  (curve tag 3); arm 1 tag 1 numbered first, arm 2 tag 2;
                  interior vertices jittered by +-10% of the local cell size.
+
+Meshes made by GMSH itself are read from its ASCII files (read_msh, formats
+4.1 and 2.2) and synthetic ones written out (write_msh) for GMSH or FRICO.
 """
 from __future__ import annotations
 
 from dataclasses import dataclass, field
+from pathlib import Path
 
 import numpy as np
 
@@ -35,6 +39,12 @@ class TriMesh:
     curves: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
     curve_tags: np.ndarray = field(default_factory=lambda: np.zeros((0,), np.int32))
     feed_tags: tuple = ()
+    # physical groups by name: (dimension, entity tags), as FRICO looks a feed up by name
+    physical: dict = field(default_factory=dict)
+
+    def entity_tags(self, name: str) -> tuple:
+        """Entity tags of a physical group (e.g. the curves of a delta-gap feed)."""
+        return tuple(self.physical[name][1])
 
     @property
     def nv(self) -> int:
@@ -218,3 +228,197 @@ def bistatic_cuts(R: float = 10.0, phis_deg=(0.0, 90.0)):
     T = np.concatenate([th for _ in phis_deg])
     P = np.concatenate([np.full(th.shape, np.radians(p)) for p in phis_deg])
     return T, P, sph2rect(R, T, P)
+
+
+# ------------------------------------------------------------------ GMSH files
+_MSH_TRIANGLE, _MSH_LINE, _MSH_POINT = 2, 1, 15
+
+
+def _msh_sections(text: str) -> dict:
+    sections, name, body = {}, None, []
+    for line in text.splitlines():
+        t = line.strip()
+        if t.startswith("$"):
+            if t.startswith("$End"):
+                sections.setdefault(name, body)
+                name, body = None, []
+            else:
+                name, body = t[1:], []
+        elif name is not None:
+            body.append(t)
+    return sections
+
+
+def _msh_physical_names(sec: dict) -> dict:
+    names = {}
+    lines = sec.get("PhysicalNames", [])
+    for line in lines[1:1 + int(lines[0])] if lines else []:
+        dim, tag, rest = line.split(maxsplit=2)
+        names[(int(dim), int(tag))] = rest.strip().strip('"')
+    return names
+
+
+def read_msh(path, skip_tags=(), name: str | None = None) -> TriMesh:
+    """A GMSH ASCII mesh file (format 4.1 or 2.2) as FRICO's load_from_gmsh takes
+    a mesh from the gmsh API (src/input_gmsh.cpp:37-210): the vertices in the
+    file's node order, the 3-node triangles of every surface entity whose tag is
+    not in skip_tags, each tagged with its surface's entity tag, and the 2-node
+    line elements tagged with their curve's entity tag (the interface tags of the
+    RWG edges they lie on). Physical groups map their names to entity tags, as a
+    delta-gap feed is named on FRICO's command line. Binary files and other
+    element types (quadrangles, second-order elements) raise ValueError."""
+    text = Path(path).read_text()
+    sec = _msh_sections(text)
+    if "MeshFormat" not in sec:
+        raise ValueError(f"{path}: not a GMSH mesh file")
+    fmt = sec["MeshFormat"][0].split()
+    version, ftype = fmt[0], int(fmt[1])
+    if ftype != 0:
+        raise ValueError(f"{path}: binary GMSH files are not supported (write ASCII)")
+    names = _msh_physical_names(sec)
+    node_tags, coords = [], []
+    tris, tri_tags, lines, line_tags = [], [], [], []
+    phys_entities: dict = {}   # (dim, physical tag) -> set of entity tags
+    skip = {int(t) for t in skip_tags}
+
+    def element(dim, etype, ent, nodes, where):
+        if etype == _MSH_TRIANGLE and dim == 2:
+            if ent not in skip:
+                tris.append(nodes[:3])
+                tri_tags.append(ent)
+        elif etype == _MSH_LINE and dim == 1:
+            lines.append(nodes[:2])
+            line_tags.append(ent)
+        elif etype != _MSH_POINT:
+            raise ValueError(f"{path}: element type {etype} on {where} is not supported "
+                             "(3-node triangles and 2-node lines only)")
+
+    if version.startswith("4"):
+        ent = sec.get("Entities", [])
+        if ent:
+            counts = [int(x) for x in ent[0].split()]
+            k = 1
+            for dim in range(4):
+                for _ in range(counts[dim]):
+                    f = ent[k].split()
+                    k += 1
+                    tag = int(f[0])
+                    np_at = 4 if dim == 0 else 7
+                    for ph in f[np_at + 1: np_at + 1 + int(f[np_at])]:
+                        phys_entities.setdefault((dim, abs(int(ph))), set()).add(tag)
+        nod = sec["Nodes"]
+        nblocks = int(nod[0].split()[0])
+        k = 1
+        for _ in range(nblocks):
+            _, _, parametric, cnt = (int(x) for x in nod[k].split())
+            k += 1
+            node_tags.extend(int(nod[k + i]) for i in range(cnt))
+            coords.extend([float(v) for v in nod[k + cnt + i].split()[:3]] for i in range(cnt))
+            k += 2 * cnt
+        el = sec["Elements"]
+        nblocks = int(el[0].split()[0])
+        k = 1
+        for _ in range(nblocks):
+            dim, etag, etype, cnt = (int(x) for x in el[k].split())
+            k += 1
+            for i in range(cnt):
+                f = [int(x) for x in el[k + i].split()]
+                element(dim, etype, etag, f[1:], f"entity ({dim}, {etag})")
+            k += cnt
+    elif version.startswith("2"):
+        nod = sec["Nodes"]
+        for line in nod[1:1 + int(nod[0])]:
+            f = line.split()
+            node_tags.append(int(f[0]))
+            coords.append([float(v) for v in f[1:4]])
+        el = sec["Elements"]
+        dims = {_MSH_TRIANGLE: 2, _MSH_LINE: 1, _MSH_POINT: 0}
+        for line in el[1:1 + int(el[0])]:
+            f = [int(x) for x in line.split()]
+            etype, ntags = f[1], f[2]
+            tags, nodes = f[3:3 + ntags], f[3 + ntags:]
+            phys = tags[0] if ntags > 0 else 0
+            etag = tags[1] if ntags > 1 else phys   # elementary (entity) tag
+            dim = dims.get(etype, -1)
+            if phys and dim >= 0:
+                phys_entities.setdefault((dim, phys), set()).add(etag)
+            element(dim, etype, etag, nodes, f"element {f[0]}")
+    else:
+        raise ValueError(f"{path}: GMSH format {version} is not supported (4.1 or 2.2)")
+
+    index = {t: i for i, t in enumerate(node_tags)}
+    try:
+        T = np.array([[index[v] for v in t] for t in tris], np.int64).reshape(-1, 3)
+        Cv = np.array([[index[v] for v in c] for c in lines], np.int64).reshape(-1, 2)
+    except KeyError as e:
+        raise ValueError(f"{path}: element refers to node {e.args[0]}, which the file does not define") from None
+    physical = {}
+    for (dim, ph), ents in sorted(phys_entities.items()):
+        physical[names.get((dim, ph), str(ph))] = (dim, tuple(sorted(ents)))
+    return TriMesh(name or Path(path).stem, np.array(coords, np.float64).reshape(-1, 3), T,
+                   np.array(tri_tags, np.int32), Cv, np.array(line_tags, np.int32), (), physical)
+
+
+def write_msh(mesh: TriMesh, path, version: str = "4.1") -> None:
+    """Write a mesh as a GMSH ASCII file (4.1 or 2.2): the triangles in blocks by
+    surface tag, the tagged curve segments by curve tag, the vertices in order
+    (tags 1..nv), and the physical groups by name. Coordinates are written with
+    17 significant digits, so read_msh gives back the same arrays."""
+    V, T, Cv = mesh.vertices, mesh.triangles, mesh.curves
+    stags = sorted(set(int(t) for t in mesh.tri_tags))
+    ctags = sorted(set(int(t) for t in mesh.curve_tags))
+    groups = list(mesh.physical.items())
+    phys_of: dict = {}   # (dim, entity tag) -> physical tags
+    for k, (_, (dim, ents)) in enumerate(groups):
+        for e in ents:
+            phys_of.setdefault((dim, int(e)), []).append(k + 1)
+    g = "{:.17g}".format
+    out = ["$MeshFormat", f"{version} 0 8", "$EndMeshFormat"]
+    if groups:
+        out += ["$PhysicalNames", str(len(groups))]
+        out += [f'{dim} {k + 1} "{nm}"' for k, (nm, (dim, _)) in enumerate(groups)]
+        out += ["$EndPhysicalNames"]
+    if version == "4.1":
+        def box(idx):
+            P = V[np.unique(idx)]
+            return " ".join(g(x) for x in (*P.min(axis=0), *P.max(axis=0)))
+
+        def entity(dim, tag, idx):
+            ph = phys_of.get((dim, tag), [])
+            return f"{tag} {box(idx)} {len(ph)}" + "".join(f" {p}" for p in ph) + " 0"
+
+        out += ["$Entities", f"0 {len(ctags)} {len(stags)} 0"]
+        out += [entity(1, t, Cv[mesh.curve_tags == t]) for t in ctags]
+        out += [entity(2, t, T[mesh.tri_tags == t]) for t in stags]
+        out += ["$EndEntities", "$Nodes", f"1 {len(V)} 1 {len(V)}", f"2 {stags[0]} 0 {len(V)}"]
+        out += [str(i + 1) for i in range(len(V))]
+        out += [" ".join(g(x) for x in v) for v in V]
+        out += ["$EndNodes", "$Elements", f"{len(ctags) + len(stags)} {len(Cv) + len(T)} 1 {len(Cv) + len(T)}"]
+        e = 0
+        for t in ctags:
+            sel = Cv[mesh.curve_tags == t]
+            out.append(f"1 {t} {_MSH_LINE} {len(sel)}")
+            for c in sel:
+                e += 1
+                out.append(f"{e} {c[0] + 1} {c[1] + 1}")
+        for t in stags:
+            sel = T[mesh.tri_tags == t]
+            out.append(f"2 {t} {_MSH_TRIANGLE} {len(sel)}")
+            for tri in sel:
+                e += 1
+                out.append(f"{e} {tri[0] + 1} {tri[1] + 1} {tri[2] + 1}")
+        out += ["$EndElements"]
+    elif version == "2.2":
+        out += ["$Nodes", str(len(V))]
+        out += [f"{i + 1} " + " ".join(g(x) for x in v) for i, v in enumerate(V)]
+        out += ["$EndNodes", "$Elements", str(len(Cv) + len(T))]
+        e = 0
+        for dim, etype, sel, tags in ((1, _MSH_LINE, Cv, mesh.curve_tags), (2, _MSH_TRIANGLE, T, mesh.tri_tags)):
+            for nodes, t in zip(sel, tags):
+                e += 1
+                ph = phys_of.get((dim, int(t)), [0])[0]
+                out.append(f"{e} {etype} 2 {ph} {int(t)} " + " ".join(str(int(v) + 1) for v in nodes))
+        out += ["$EndElements"]
+    else:
+        raise ValueError(f"GMSH format {version} is not written (4.1 or 2.2)")
+    Path(path).write_text("\n".join(out) + "\n")
