@@ -112,6 +112,23 @@ def test_abi_exports_every_declared_symbol(gpu_lib):
         assert hasattr(lib, nm), nm
 
 
+def test_abi_constants_match_header():
+    """Every integer constant the Python binding mirrors has the header's value."""
+    from frico_gb300 import _abi
+    header = (ROOT / "include" / "frico_gpu.h").read_text()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+FRICO_(\w+)\s+(-?\d+)\b", header)}
+    mirrored = 0
+    for name, value in defs.items():
+        key = name[len("GPU_"):] if name.startswith("GPU_") else name
+        if hasattr(_abi, key):
+            assert getattr(_abi, key) == value, name
+            mirrored += 1
+    for group in ("GEMM_", "PIVOT_", "REFINE_", "RESIDUAL_", "PREC_", "HPHASE_", "EDGE_LENGTH_"):
+        names = [n for n in defs if n.startswith(group)]
+        assert names and all(hasattr(_abi, n) for n in names), group
+    assert mirrored >= 25
+
+
 def test_build_can_be_called_again_in_one_process(gpu_lib):
     import frico_gb300
     frico_gb300.build()
