@@ -38,9 +38,14 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
+def reference_dir() -> Path:
+    """The FRICO checkout whose sources pin the oracle (FRICO_REFERENCE overrides)."""
+    return Path(os.environ.get("FRICO_REFERENCE", "/root/reference"))
+
+
 def build_ref() -> Path | None:
     """Compile FRICO's own sources (where they lie) into oracle/_ref/, if present."""
-    ref = Path(os.environ.get("FRICO_REFERENCE", "/root/reference"))
+    ref = reference_dir()
     if not (ref / "src" / "quadratures.cpp").exists() or not (HERE / "ref" / "Makefile").exists():
         return None
     r = subprocess.run(["make", "-s", "-C", str(HERE / "ref"), f"REF={ref}"], capture_output=True, text=True)
