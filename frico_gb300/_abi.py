@@ -98,6 +98,7 @@ PROTOTYPES = {
     "frico_gpu_lump_currents": [P, I32, P, P, P],
     "frico_gpu_eval_fields": [P, I32, I64, P, P, P],
     "frico_gpu_eval_fields_noalloc": [P, I32, I64, P, P, P],
+    "frico_gpu_set_matrix": [P, P, I64],
     "frico_gpu_sweep": [P, I32, P, I32, P, C128, P, I32, P, I64, P, I32, P, P, P, P],
     "frico_gpu_adjoint": [P, D, I32, P, C128, P, P, I32, P, P, P, P],
     "frico_gpu_eval_fields_multi": [P, I32, I32, I64, P, P, P],

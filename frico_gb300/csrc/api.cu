@@ -296,6 +296,26 @@ extern "C" int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out
     return rc;
 }
 
+extern "C" int frico_gpu_set_matrix(frico_gpu_ctx* ctx, const frico_c128* Z, int64_t ldz) {
+    FRICO_CTX_CHECK(ctx);
+    if (ctx->n <= 0) return set_err(ctx, FRICO_GPU_ESTATE, "set_matrix: no mesh");
+    if (!Z || ldz < ctx->n) return set_err(ctx, FRICO_GPU_EINVAL, "set_matrix: null Z or ldz < n");
+    const int64_t n = ctx->n;
+    int rc = ensure(ctx, ctx->z64, sizeof(double2) * size_t(n) * size_t(n));
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpy2DAsync(ctx->z64.p, sizeof(double2) * n, Z, sizeof(frico_c128) * ldz,
+                                               sizeof(double2) * n, n, cudaMemcpyHostToDevice, ctx->stream),
+                        "upload Z");
+    if (!rc && ctx->opt.precision == FRICO_PREC_MIXED) rc = z64_to_z32(ctx);
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "set_matrix sync");
+    if (rc) return rc;
+    ctx->z_valid = true;
+    ctx->z_df = false;   // an FP64 Z as given: nothing to reassemble before an FP64 fallback
+    ctx->factored = ctx->solved = false;
+    ctx->lumped_col = -1;
+    return FRICO_GPU_OK;
+}
+
 extern "C" int frico_gpu_set_nrhs(frico_gpu_ctx* ctx, int32_t nrhs) {
     FRICO_CTX_CHECK(ctx);
     if (ctx->n <= 0) return set_err(ctx, FRICO_GPU_ESTATE, "set_nrhs: no mesh");

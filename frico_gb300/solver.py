@@ -172,6 +172,14 @@ class Simulation:
         self.freq = float(freq)
         return Z
 
+    def set_matrix(self, Z: np.ndarray):
+        """A Z assembled elsewhere (n x n complex) in place of compute_matrix; solve()
+        then factors it, as FRICO's solve_general takes its matrix argument."""
+        Zf = np.asarray(Z, np.complex128, order="F")
+        if Zf.shape != (self.n, self.n):
+            raise ValueError(f"set_matrix: Z must be {self.n} x {self.n}")
+        self._call("frico_gpu_set_matrix", ptr(Zf), self.n)
+
     def set_nrhs(self, nrhs: int):
         self._call("frico_gpu_set_nrhs", int(nrhs))
         self.nrhs = int(nrhs)

@@ -186,6 +186,13 @@ int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* xyz,
  * if Z_out != NULL it is also copied there (column-major, leading dim ldz >= n). */
 int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out, int64_t ldz);
 
+/* Replaces the matrix argument A of solve_general / solve_symmetric
+ * (src/lapack_wrappers.h:10-19) for a Z the caller assembled itself: upload the
+ * n x n complex matrix (column-major, leading dim ldz >= n, n = the mesh's RWG
+ * count) in place of a fill; the next frico_gpu_solve factors it (for
+ * FRICO_PREC_MIXED, a complex64 copy refined against this FP64 Z). */
+int frico_gpu_set_matrix(frico_gpu_ctx* ctx, const frico_c128* Z, int64_t ldz);
+
 /* Set the right-hand-side count (columns of V); resets V to zero. */
 int frico_gpu_set_nrhs(frico_gpu_ctx* ctx, int32_t nrhs);
 /* update_rhs(delta_gap): V[:,col] += (-j l/(omega mu0)) V0 sign on feed edges.

@@ -314,6 +314,27 @@ def test_mixed_unpivoted_factors(gpu_lib, level, engine):
     assert rel_norm(L @ U, Zr) < (1e-2 if engine == "tc_f16" else 1e-4)   # measured 1.2e-5 (tensor cores)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_set_matrix_solves_a_given_z(gpu_lib, sphere2, precision):
+    """frico_gpu_set_matrix: a Z assembled elsewhere (here the oracle's) is solved
+    as FRICO's solve_general solves its matrix argument; a second upload replaces
+    the first (and its factors)."""
+    f = 450e6
+    o = oracle_for(sphere2)
+    Zr = o.compute_matrix(f)
+    rng = np.random.default_rng(11)
+    B = rng.standard_normal((o.n, 3)) + 1j * rng.standard_normal((o.n, 3))
+    Xr = np.linalg.solve(Zr, B)
+    tol = OUT_TOL if precision == "fp64" else MIXED_TOL
+    sim = Simulation(sphere2, precision=precision)
+    sim.set_matrix(Zr)
+    sim.set_rhs(B)
+    assert rel_norm(sim.solve(), Xr) < tol
+    sim.set_matrix(2.0 * Zr)
+    sim.set_rhs(B)
+    assert rel_norm(sim.solve(), 0.5 * Xr) < tol
+
+
 def test_singular_matrix_info(gpu_lib):
     """The xy-hypot edge length makes vertical edges zero-length: Z gets zero
     rows/columns and zgetrf reports the first zero pivot; so must the GPU."""
