@@ -335,6 +335,34 @@ def test_set_matrix_solves_a_given_z(gpu_lib, sphere2, precision):
     assert rel_norm(sim.solve(), 0.5 * Xr) < tol
 
 
+def test_sphere_l4_mixed_matches_fp64_at_full_size(gpu_lib):
+    """The headline workload at its full size (7680 unknowns, 450 MHz, 181 x 2
+    bistatic points): the mixed path's currents, far field and sigma agree with the
+    FP64 drop-in's to the 1e-6 the metric requires, and its refinement reaches the
+    FP64 residual tolerance."""
+    m = meshes.icosphere(4)
+    f = 450e6
+    pw = PlaneWave(0.0, 0.0, 1.0, 0.0)
+    T, P, pts = meshes.bistatic_cuts(10.0)
+    out = {}
+    for precision in ("fp64", "mixed"):
+        sim = Simulation(m, precision=precision)
+        sim.compute_matrix(f)
+        sim.set_nrhs(1)
+        sim.update_rhs(f, pw)
+        I = sim.solve()[:, 0]
+        st = sim.stats()
+        E, _ = sim.eval_fields(pts)
+        out[precision] = (I, E, sim.rcs_points(10.0, T, P), st)
+        sim.close()
+    I64, E64, s64, _ = out["fp64"]
+    Imx, Emx, smx, st = out["mixed"]
+    assert st["precision_used"] == 1 and st["refine_residual"] <= 1e-12
+    assert rel_norm(Imx, I64) < 1e-6
+    assert rel_norm(Emx, E64) < 1e-6
+    assert np.max(np.abs(smx - s64)) / np.max(np.abs(s64)) < 1e-6
+
+
 def test_singular_matrix_info(gpu_lib):
     """The xy-hypot edge length makes vertical edges zero-length: Z gets zero
     rows/columns and zgetrf reports the first zero pivot; so must the GPU."""
