@@ -363,6 +363,24 @@ def test_sphere_l4_mixed_matches_fp64_at_full_size(gpu_lib):
     assert np.max(np.abs(smx - s64)) / np.max(np.abs(s64)) < 1e-6
 
 
+def test_force_symmetry(gpu_lib, strip):
+    """-S (src/emw_solver.h:118-120): Z <- (Z + Z^T) / 2 before the solve, against
+    the oracle's Z symmetrised the same way and LAPACK's solve_symmetric on it."""
+    f = 300e6
+    o = oracle_for(strip)
+    Zr = o.compute_matrix(f)
+    Zs = (Zr + Zr.T) / 2
+    Vr = o.rhs_delta_gap(f, [meshes.FEED_TAG])
+    Ir = o.solve(Zs, Vr, symmetric=True)
+    sim = Simulation(strip, force_symmetry=True)
+    Z = sim.compute_matrix(f, download=True)
+    assert np.abs(Z - Z.T).max() == 0.0
+    assert np.abs(Z - Zs).max() / np.abs(Zs).max() < 1e-10
+    sim.set_nrhs(1)
+    sim.update_rhs(f, DeltaGap((meshes.FEED_TAG,)))
+    assert rel_norm(sim.solve()[:, 0], Ir) < OUT_TOL
+
+
 def test_singular_matrix_info(gpu_lib):
     """The xy-hypot edge length makes vertical edges zero-length: Z gets zero
     rows/columns and zgetrf reports the first zero pivot; so must the GPU."""
