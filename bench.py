@@ -48,7 +48,9 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--level", type=int, default=4, help="icosphere level (4: N=7680)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 accuracy check")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64 GPU drop-in run (its solves/s and the mixed-vs-FP64 accuracy)")
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the FP64 GPU drop-in")
     ap.add_argument("--gemm-engine", default="auto", choices=["auto", "simt", "tc", "tc_f16"],
                     help="auto/tc: 3xTF32 operands; tc_f16: 3xFP16 block columns of the unpivoted LU")
     ap.add_argument("--pivoting", default="auto", choices=["auto", "partial", "none"])
@@ -79,11 +81,14 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = None
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            import tempfile
+            fd, name = tempfile.mkstemp(prefix="frico_clocks_", suffix=".csv")
+            os.close(fd)
+            self.path = Path(name)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -114,6 +119,10 @@ class ClockSampler:
             for nm, v in zip(names, p[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
@@ -128,17 +137,18 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+# DRAM traffic (ncu: dram__bytes_read.sum + dram__bytes_write.sum) per launch of the complex64
+# LU's narrow and trailing-update GEMMs, averaged over every update launch of one L4-sphere
+# solve; the capture and its command are summarised in profiles/k_gemm_tf32x3_sphere_L4_mixed.md.
+GEMM_TRAFFIC_BYTES_PER_LAUNCH = {("k_gemm_tf32x3", 4): 157.3e6}
+
+
 def gemm_traffic_per_launch(level: int, precision: str, kernel: str):
-    """DRAM bytes per narrow / trailing-update launch of the complex64 LU from one
-    ncu capture (dram__bytes_read.sum + dram__bytes_write.sum over all of a
-    solve's update launches), recorded with its command in
-    profiles/<kernel>_sphere_L4_mixed.md; None for other configurations."""
-    p = ROOT / "profiles" / f"{kernel}_sphere_L4_mixed.md"
-    if level != 4 or precision != "mixed" or not p.exists():
+    """Measured DRAM bytes per update launch for the configuration the capture was
+    made on (the L4 sphere, mixed precision); None for any other."""
+    if precision != "mixed":
         return None
-    import re
-    m = re.search(r"traffic_bytes_per_launch = ([0-9.eE+]+)", p.read_text())
-    return float(m.group(1)) if m else None
+    return GEMM_TRAFFIC_BYTES_PER_LAUNCH.get((kernel, level))
 
 
 # ------------------------------------------------------------------ CPU paths
@@ -377,21 +387,43 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": roof, "clocks": clk}
     if rank == 0 and args.precision == "mixed" and not args.no_accuracy:
-        # the metric's accuracy condition: mixed vs the FP64 GPU path on the same inputs
+        # the metric's reference point, the plain FP64 GPU drop-in on the same workload in the
+        # same run: one untimed step (which also gives the accuracy reference), then
+        # `fp64_steps` timed steps with CUDA events on its stream
+        ref = Simulation(mesh, precision="fp64", device=local)
+        rstream = C.c_void_p()
+        lib.frico_gpu_get_stream(ref.ctx, C.byref(rstream))
+        rext = torch.cuda.ExternalStream(rstream.value, device=local)
+
+        def step64():
+            ref.compute_matrix(FREQ)
+            ref.set_nrhs(1)
+            ref.update_rhs(FREQ, pw)
+            ref.solve(download=False)
+            return ref.rcs_points(R_FAR, T, P)
+
+        step64()
+        I_64 = ref.solve()[:, 0]      # factors kept: the solve is repeated, not refactored
+        sig_64 = ref.rcs_points(R_FAR, T, P)
+        E_64, _ = ref.eval_fields(meshes.sph2rect(R_FAR, T, P))
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(rext)
+        for _ in range(args.fp64_steps):
+            step64()
+        f1.record(rext)
+        torch.cuda.synchronize()
+        fp64_value = args.fp64_steps / (f0.elapsed_time(f1) / 1000.0)
+        ref.close()
+        line["fp64_gpu_value"] = fp64_value
+        line["fp64_gpu_steps"] = args.fp64_steps
+        line["mixed_over_fp64"] = value / fp64_value
         sim.compute_matrix(FREQ)
         sim.set_nrhs(1)
         sim.update_rhs(FREQ, pw)
         I_mx = sim.solve()[:, 0]
         sig_mx = sim.rcs_points(R_FAR, T, P)
-        ref = Simulation(mesh, precision="fp64", device=local)
-        ref.compute_matrix(FREQ)
-        ref.set_nrhs(1)
-        ref.update_rhs(FREQ, pw)
-        I_64 = ref.solve()[:, 0]
-        sig_64 = ref.rcs_points(R_FAR, T, P)
         E_mx, _ = sim.eval_fields(meshes.sph2rect(R_FAR, T, P))
-        E_64, _ = ref.eval_fields(meshes.sph2rect(R_FAR, T, P))
-        ref.close()
         line["accuracy_vs_fp64_gpu"] = {
             "currents_rel_l2": float(np.linalg.norm(I_mx - I_64) / np.linalg.norm(I_64)),
             "far_field_E_rel_l2": float(np.linalg.norm(E_mx - E_64) / np.linalg.norm(E_64)),
@@ -692,6 +724,18 @@ def run_sphere64(args):
             "e2e": {"value": args.steps / sec, "unit": "solves/s", "h2d_bytes_per_step": int(16 * T.shape[0]),
                     "d2h_bytes_per_step": int(sig.nbytes)},
             "clocks": clk}
+    if args.precision == "mixed" and not args.no_accuracy:
+        # the field pass's engine (tensor-core GEMMs for many columns on the mixed path) against the
+        # direct double-float kernels on 2000 seeded points of the grid, every incidence
+        idx = np.random.default_rng(5).choice(T.size, 2000, replace=False)
+        sim.set_options(fields_engine=1)
+        sig_d = sim.rcs_points_multi(R_FAR, T[idx], Pg[idx])
+        sim.set_options(fields_engine=0)
+        sig_s = sig[:, idx]
+        line["fields_vs_direct"] = {
+            "sigma_rel_max": float(max(np.abs(sig_s[c] - sig_d[c]).max() / np.abs(sig_d[c]).max()
+                                       for c in range(nrhs))),
+            "points": 2000, "engine": "tensor-core GEMM (auto)", "bound": 1e-6}
     print(json.dumps(line), flush=True)
     sim.close()
 

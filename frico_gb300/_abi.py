@@ -22,6 +22,7 @@ GEMM_AUTO, GEMM_SIMT, GEMM_TC, GEMM_TC_F16 = 0, 1, 2, 3
 PIVOT_AUTO, PIVOT_PARTIAL, PIVOT_NONE = 0, 1, 2
 REFINE_AUTO, REFINE_CLASSIC = 0, 1
 RESIDUAL_AUTO, RESIDUAL_FP64 = 0, 1
+FIELDS_AUTO, FIELDS_DIRECT, FIELDS_GEMM = 0, 1, 2
 
 # numpy mirror of frico_rwg (112 bytes)
 RWG_DTYPE = np.dtype([
@@ -41,7 +42,7 @@ class Options(C.Structure):
                 ("precision", C.c_int32), ("h_phase_mode", C.c_int32), ("max_refine_iters", C.c_int32),
                 ("refine_tol", C.c_double), ("Z0", C.c_double), ("profile_kernels", C.c_int32),
                 ("gemm_engine", C.c_int32), ("pivoting", C.c_int32), ("refine_mode", C.c_int32),
-                ("residual_mode", C.c_int32)]
+                ("residual_mode", C.c_int32), ("wait_limit_cycles", C.c_int64), ("fields_engine", C.c_int32)]
 
 
 class PortValues(C.Structure):
@@ -98,7 +99,7 @@ PROTOTYPES = {
     "frico_gpu_lump_currents": [P, I32, P, P, P],
     "frico_gpu_eval_fields": [P, I32, I64, P, P, P],
     "frico_gpu_eval_fields_noalloc": [P, I32, I64, P, P, P],
-    "frico_gpu_set_matrix": [P, P, I64],
+    "frico_gpu_set_matrix": [P, D, P, I64],
     "frico_gpu_sweep": [P, I32, P, I32, P, C128, P, I32, P, I64, P, I32, P, P, P, P],
     "frico_gpu_adjoint": [P, D, I32, P, C128, P, P, I32, P, P, P, P],
     "frico_gpu_eval_fields_multi": [P, I32, I32, I64, P, P, P],
@@ -109,6 +110,7 @@ PROTOTYPES = {
     "frico_gpu_rcs_points": [P, I32, D, I64, P, P, P],
     "frico_gpu_last_stats": [P, P],
     "frico_gpu_debug_cgemm": [P, I32, I32, I32, P, P, P, I32],
+    "frico_gpu_debug_z64": [P, P, P],
 }
 
 _lib = None

@@ -15,6 +15,7 @@
 #include <new>
 
 #include "common.cuh"
+#include "frico_gpu_debug.h"
 
 namespace frico {
 
@@ -81,6 +82,8 @@ static int check_options(frico_gpu_ctx* ctx, const frico_gpu_options* o) {
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown refine_mode");
     if (o->residual_mode != FRICO_RESIDUAL_AUTO && o->residual_mode != FRICO_RESIDUAL_FP64)
         return set_err(ctx, FRICO_GPU_EINVAL, "unknown residual_mode");
+    if (o->fields_engine < FRICO_FIELDS_AUTO || o->fields_engine > FRICO_FIELDS_GEMM)
+        return set_err(ctx, FRICO_GPU_EINVAL, "unknown fields_engine");
     return FRICO_GPU_OK;
 }
 
@@ -149,7 +152,7 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
                       &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws,   &ctx->lut,       &ctx->dinv_t,
                       &ctx->adj_ws,  &ctx->adj_tab, &ctx->mlump,     &ctx->mfld,     &ctx->gm_ws,
-                      &ctx->dinv128, &ctx->trsv_x};
+                      &ctx->dinv128, &ctx->trsv_x, &ctx->ffws};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -285,6 +288,7 @@ extern "C" int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out
     }
     if (rc) return rc;
     ctx->z_valid = true;
+    ctx->z32_stale = false;
     ctx->factored = ctx->solved = false;
     ctx->lumped_col = -1;
     if (Z_out) {
@@ -296,20 +300,25 @@ extern "C" int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out
     return rc;
 }
 
-extern "C" int frico_gpu_set_matrix(frico_gpu_ctx* ctx, const frico_c128* Z, int64_t ldz) {
+extern "C" int frico_gpu_set_matrix(frico_gpu_ctx* ctx, double freq, const frico_c128* Z, int64_t ldz) {
     FRICO_CTX_CHECK(ctx);
     if (ctx->n <= 0) return set_err(ctx, FRICO_GPU_ESTATE, "set_matrix: no mesh");
     if (!Z || ldz < ctx->n) return set_err(ctx, FRICO_GPU_EINVAL, "set_matrix: null Z or ldz < n");
+    if (!(freq > 0) || !std::isfinite(freq)) return set_err(ctx, FRICO_GPU_EINVAL, "set_matrix: frequency must be > 0");
     const int64_t n = ctx->n;
     int rc = ensure(ctx, ctx->z64, sizeof(double2) * size_t(n) * size_t(n));
     if (!rc)
         rc = cuda_check(ctx, cudaMemcpy2DAsync(ctx->z64.p, sizeof(double2) * n, Z, sizeof(frico_c128) * ldz,
                                                sizeof(double2) * n, n, cudaMemcpyHostToDevice, ctx->stream),
                         "upload Z");
+    // solve_symmetric (zsytrf, uplo = 'U') reads only the upper triangle of its argument
+    if (!rc && (ctx->opt.approx || ctx->opt.force_symmetry)) rc = mirror_upper(ctx);
     if (!rc && ctx->opt.precision == FRICO_PREC_MIXED) rc = z64_to_z32(ctx);
     if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "set_matrix sync");
     if (rc) return rc;
+    ctx->freq = freq;
     ctx->z_valid = true;
+    ctx->z32_stale = false;
     ctx->z_df = false;   // an FP64 Z as given: nothing to reassemble before an FP64 fallback
     ctx->factored = ctx->solved = false;
     ctx->lumped_col = -1;
@@ -403,6 +412,9 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
                                          (mixed && ctx->factor_prec == FRICO_PREC_FP64));
     if (!reuse) {
         if (!ctx->z_valid) return set_err(ctx, FRICO_GPU_ESTATE, "solve: no impedance matrix (call fill)");
+        // a factorisation that stopped part-way left its in-place copy half factored
+        if (mixed && ctx->z32_stale && (rc = z64_to_z32(ctx))) return rc;
+        ctx->z32_stale = false;
         if (mixed) {
             rc = factor_mixed(piv == FRICO_PIVOT_PARTIAL);
             if (!rc && ctx->info != 0 && piv == FRICO_PIVOT_AUTO) {
@@ -414,7 +426,12 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
             rc = lu_factor_fp64(ctx);
             ctx->stats.pivoting_used = FRICO_PIVOT_PARTIAL;
         }
-        if (rc) return rc;
+        if (rc) {
+            // the factorisation works in place: Z64 (FP64) or the complex64 copy is no longer Z
+            if (mixed) ctx->z32_stale = true;
+            else ctx->z_valid = false;
+            return rc;
+        }
         ctx->factored = true;
         ctx->factor_prec = ctx->opt.precision;
         if (!mixed) ctx->z_valid = false;  // Z64 now holds the LU factors, as zgetrf leaves A
@@ -561,8 +578,11 @@ extern "C" int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t np
 // Device-pointer, allocation-free form of frico_gpu_eval_fields (no FRICO
 // counterpart). Every pointer is checked to be device memory of the context's
 // device before anything is launched, so a host pointer comes back as EINVAL.
-static int check_device_ptr(frico_gpu_ctx* ctx, const void* p, const char* what) {
+static int check_device_ptr(frico_gpu_ctx* ctx, const void* p, const char* what, uintptr_t align) {
     if (!p) return FRICO_GPU_OK;
+    if (uintptr_t(p) % align != 0)
+        return set_err(ctx, FRICO_GPU_EINVAL, std::string("eval_fields_noalloc: ") + what + " is not " +
+                                                  std::to_string(align) + "-byte aligned");
     cudaPointerAttributes a{};
     cudaError_t e = cudaPointerGetAttributes(&a, p);
     if (e != cudaSuccess) {
@@ -583,8 +603,9 @@ extern "C" int frico_gpu_eval_fields_noalloc(frico_gpu_ctx* ctx, int32_t col, in
     if (!ctx->solved) return set_err(ctx, FRICO_GPU_ESTATE, "eval_fields_noalloc: not solved");
     if (npts <= 0 || !P_dev || (!E_dev && !H_dev))
         return set_err(ctx, FRICO_GPU_EINVAL, "eval_fields_noalloc: need npts > 0, P_dev and E_dev or H_dev");
-    if ((rc = check_device_ptr(ctx, P_dev, "P_dev")) || (rc = check_device_ptr(ctx, E_dev, "E_dev")) ||
-        (rc = check_device_ptr(ctx, H_dev, "H_dev")))
+    if ((rc = check_device_ptr(ctx, P_dev, "P_dev", alignof(double))) ||
+        (rc = check_device_ptr(ctx, E_dev, "E_dev", alignof(double2))) ||
+        (rc = check_device_ptr(ctx, H_dev, "H_dev", alignof(double2))))
         return rc;
     return eval_fields_noalloc(ctx, col, npts, P_dev, (double2*)E_dev, (double2*)H_dev);
 }
@@ -778,6 +799,14 @@ extern "C" int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, i
     release(buf);
     if (!rc && hs.err == FRICO_DEV_ERR_TIMEOUT) rc = set_err(ctx, FRICO_GPU_ETIMEOUT, "tensor-core GEMM wait timed out");
     return rc;
+}
+
+extern "C" int frico_gpu_debug_z64(frico_gpu_ctx* ctx, const void** dev_ptr, int64_t* ld) {
+    if (!ctx || !dev_ptr || !ld) return FRICO_GPU_EINVAL;
+    if (!ctx->z_valid || !ctx->z64.p) return set_err(ctx, FRICO_GPU_ESTATE, "debug_z64: no FP64 Z resident");
+    *dev_ptr = ctx->z64.p;
+    *ld = ctx->n;
+    return FRICO_GPU_OK;
 }
 
 extern "C" int frico_gpu_last_stats(frico_gpu_ctx* ctx, frico_gpu_stats* stats) {

@@ -187,6 +187,7 @@ struct frico_gpu_ctx {
     double freq = 0.0;
     bool z_valid = false;         // Z64 holds the matrix of `freq`
     bool z_df = false;            // ... assembled in double-float (mixed precision only)
+    bool z32_stale = false;       // z32 no longer holds Z (a factorisation stopped part-way)
     frico::DevBuf gtab, smom, basis_aux, z64, z32;
 
     // factorisation / solve
@@ -211,6 +212,7 @@ struct frico_gpu_ctx {
     // adjoint: transposed factors, their inverted diagonal blocks, workspaces
     frico::DevBuf lut, dinv_t, adj_ws, adj_tab;
     frico::DevBuf mlump, mfld;    // multi-column lumped currents and field partial sums
+    frico::DevBuf ffws;           // far field as GEMMs: chunk operands, chunk results, FP64 sums
     frico::DevBuf gm_ws;          // GMRES refinement: Arnoldi basis and work vectors
     int32_t lumped_col = -1;
 
@@ -250,6 +252,12 @@ struct StageTimer {
 enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceTrsv128, kOnceKeys };
 int device_once(frico_gpu_ctx* ctx, OnceKey key, int (*init)(frico_gpu_ctx*));
 
+// Limit of the device-side waits on other CTAs (chained solves, grid barrier), in SM cycles.
+static const long long kDefaultWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
+inline long long wait_limit(const frico_gpu_ctx* ctx) {
+    return ctx->opt.wait_limit_cycles > 0 ? (long long)ctx->opt.wait_limit_cycles : kDefaultWaitCycles;
+}
+
 // Count one kernel launch on the context (reported as stats.kernel_launches).
 inline void count_launch(frico_gpu_ctx* ctx, int64_t k = 1) { ctx->stats.kernel_launches += k; }
 
@@ -257,6 +265,7 @@ inline void count_launch(frico_gpu_ctx* ctx, int64_t k = 1) { ctx->stats.kernel_
 int build_quadrature(frico_gpu_ctx* ctx);                     // fill.cu
 int fill_matrix(frico_gpu_ctx* ctx, double freq, bool fp64_only = false);   // fill.cu
 int symmetrize(frico_gpu_ctx* ctx);                           // fill.cu
+int mirror_upper(frico_gpu_ctx* ctx);                         // fill.cu
 int lu_factor_fp64(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_factor_fp32(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb);   // lu.cu
@@ -301,6 +310,13 @@ struct TcDiagSplit {
     float* res_u12;
 };
 size_t tc_panel_ws_bytes(int64_t n);
+int gemm_tc_split_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, float* C1, int64_t ldc1, int N1,
+                       const float* A1h, const float* A1l, const float* B1h, const float* B1l, float* C2,
+                       int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
+                       const float* B2l);   // gemm_tc.cu
+bool fields_gemm_available(frico_gpu_ctx* ctx);                // fields_gemm.cu
+int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* dP, const double2* AJ,
+                     const double2* AD, double2* E_dev, int kc);   // fields_gemm.cu
 int tc_diag_split_slots(frico_gpu_ctx* ctx, TcDiagSplit* out);
 int tc_lu_scale(frico_gpu_ctx* ctx, const float2* A, int64_t lda, int n);
 int tc_lu_panel_split(frico_gpu_ctx* ctx, float2* A, int64_t lda, int k0, int jb, int rest);

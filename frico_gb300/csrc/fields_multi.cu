@@ -307,6 +307,27 @@ int eval_fields_multi(frico_gpu_ctx* ctx, int col0, int ncols, int64_t npts, con
             return rc;
     }
     const bool with_h = H_host != nullptr;
+    const int fe = ctx->opt.fields_engine;
+    const bool gemm = !with_h && (fe == FRICO_FIELDS_GEMM ||
+                                  (fe == FRICO_FIELDS_AUTO && ctx->opt.precision == FRICO_PREC_MIXED && ncols >= 4 &&
+                                   fields_gemm_available(ctx)));
+    if (fe == FRICO_FIELDS_GEMM && !fields_gemm_available(ctx))
+        return set_err(ctx, FRICO_GPU_EINVAL, "fields GEMM: tensor cores (tcgen05) not available on this device");
+    if (gemm) {
+        // E as tensor-core GEMMs: points and E on the device, in the field workspace
+        const int64_t cnt = int64_t(ncols) * npts * 3;
+        if ((rc = ensure(ctx, ctx->mfld, sizeof(double2) * cnt + sizeof(double) * 3 * npts + 256))) return rc;
+        double2* Ed = (double2*)ctx->mfld.p;
+        double* dP = (double*)(Ed + cnt);
+        if ((rc = cuda_check(ctx, cudaMemcpyAsync(dP, P_host, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st),
+                             "points")))
+            return rc;
+        if ((rc = eval_fields_gemm(ctx, ncols, npts, dP, AJ, AD, Ed, 0))) return rc;
+        if ((rc = cuda_check(ctx, cudaMemcpyAsync(E_host, Ed, sizeof(double2) * cnt, cudaMemcpyDeviceToHost, st),
+                             "fields out")))
+            return rc;
+        return cuda_check(ctx, cudaStreamSynchronize(st), "fields sync");
+    }
     const int nper = with_h ? 6 : 3;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);

@@ -550,6 +550,26 @@ __global__ void k_symmetrize(int64_t n, int64_t ld, double2* Z) {
     }
 }
 
+// Lower triangle <- transpose of the upper one: Z[r][c] = Z[c][r] for r > c, the
+// matrix zsytrf with uplo = 'U' factors (src/lapack_wrappers.cpp:135-177).
+// Block (bx, by) writes the 32 x 32 tile at rows 32 by, columns 32 bx (by >= bx)
+// from the mirror tile, staged through shared memory.
+__global__ void k_mirror_upper(int64_t n, int64_t ld, double2* Z) {
+    __shared__ double2 t[32][33];
+    const int64_t bi = blockIdx.y, bj = blockIdx.x;
+    if (bi < bj) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t row = bj * 32 + r, col = bi * 32 + tx;   // upper source tile
+        t[r][tx] = (row < n && col < n) ? Z[col * ld + row] : make_double2(0, 0);
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t row = bi * 32 + r, col = bj * 32 + tx;
+        if (row < n && col < n && row > col) Z[col * ld + row] = t[tx][r];
+    }
+}
+
 // Z[j, i] of the degree-1 fill (mode 0) for basis i (column) and test j (row).
 __device__ __forceinline__ double2 entry_mode0(const AsmArgs& A, const BasisAsm& bi, const BasisAsm& bj,
                                                int64_t i) {
@@ -834,6 +854,14 @@ int z64_to_z32(frico_gpu_ctx* ctx) {
                                                                        (float2*)ctx->z32.p);
     count_launch(ctx);
     return cuda_check(ctx, cudaGetLastError(), "k_z64_to_z32");
+}
+
+int mirror_upper(frico_gpu_ctx* ctx) {
+    const int64_t n = ctx->n;
+    const unsigned nb = unsigned((n + 31) / 32);
+    k_mirror_upper<<<dim3(nb, nb), dim3(32, 8), 0, ctx->stream>>>(n, n, (double2*)ctx->z64.p);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_mirror_upper");
 }
 
 int symmetrize(frico_gpu_ctx* ctx) {

@@ -181,6 +181,7 @@ struct GemmProb {
     int64_t ldc;
     int M, N;          // real rows (2 x complex rows), columns
     int tiles_m, tiles;
+    int nfast;         // 1: consecutive tiles walk N first (A tile reused from L2), else M first
     int accumulate;    // 1: C -= A B; 0: C = A B
     int emit;          // 0, 1 (A*) or 2 (B^), into eh / el with rows of KP operand values
     void* eh;          // float (3xTF32) or __half (3xFP16) operands
@@ -268,8 +269,9 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int pi = t >= g.p[0].tiles ? 1 : 0;
-                const int tt = t - (pi ? g.p[0].tiles : 0), tm = pi ? g.p[1].tiles_m : g.p[0].tiles_m;
-                const int mt = tt % tm, nt_ = tt / tm;
+                const GemmProb& PP = pi ? g.p[1] : g.p[0];
+                const int tt = t - (pi ? g.p[0].tiles : 0), tm = PP.tiles_m, tn = PP.tiles / PP.tiles_m;
+                const int mt = PP.nfast ? tt / tn : tt % tm, nt_ = PP.nfast ? tt % tn : tt / tm;
                 const CUtensorMap* mAh = pi ? &tmAh1 : &tmAh0;
                 const CUtensorMap* mAl = pi ? &tmAl1 : &tmAl0;
                 const CUtensorMap* mBh = pi ? &tmBh1 : &tmBh0;
@@ -334,8 +336,8 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
             const int acc = tcount & 1, around = tcount >> 1;
             const int pi = t >= g.p[0].tiles ? 1 : 0;
             const GemmProb P = pi ? g.p[1] : g.p[0];
-            const int tt = t - (pi ? g.p[0].tiles : 0);
-            const int mt = tt % P.tiles_m, nt_ = tt / P.tiles_m;
+            const int tt = t - (pi ? g.p[0].tiles : 0), tn = P.tiles / P.tiles_m;
+            const int mt = P.nfast ? tt / tn : tt % P.tiles_m, nt_ = P.nfast ? tt % tn : tt / P.tiles_m;
             const int gr = mt * BM + row;
             const int ncol = min(64, P.N - nt_ * BN - h);   // columns of this warp's half (may be <= 0)
             const bool rowok = gr < P.M;
@@ -650,6 +652,7 @@ static int make_problem(frico_gpu_ctx* ctx, TcProblem& q, float2* C, int64_t ldc
     q.p.N = N;
     q.p.tiles_m = (M + tc::BM - 1) / tc::BM;
     q.p.tiles = q.p.tiles_m * ((N + 127) / 128);
+    q.p.nfast = 0;
     q.p.accumulate = accumulate;
     q.p.emit = emit;
     q.p.eh = eh;
@@ -728,6 +731,29 @@ int gemm_update_tc(frico_gpu_ctx* ctx, float2* C, int64_t ldc, const float2* L, 
                            f16 ? &rs : nullptr)))
         return rc;
     return launch_gemm(ctx, st, &q, 1, KP, max_ctas, ev);
+}
+
+// Two independent real products C_i = A_i B_i^T (overwrite, no accumulation) in one
+// launch, from operands already split into TF32 hi / lo, K-major: A_i with M rows, B_i with
+// N_i rows, KP values per row (a multiple of 32). C_i is real, M x N_i, column-major with
+// leading dimension ldc_i floats. Consecutive tiles walk N first, so the CTAs working on
+// the N tiles of one A tile run together and read it once from DRAM.
+int gemm_tc_split_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, float* C1, int64_t ldc1, int N1,
+                       const float* A1h, const float* A1l, const float* B1h, const float* B1l, float* C2,
+                       int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
+                       const float* B2l) {
+    if (KP % tc::BK != 0 || M <= 0 || N1 <= 0 || N2 <= 0 || ldc1 < M || ldc2 < M)
+        return set_err(ctx, FRICO_GPU_EINVAL, "gemm_tc_split_pair: bad shape");
+    TcProblem q[2];
+    int rc;
+    if ((rc = make_problem(ctx, q[0], (float2*)C1, 0, M, N1, A1h, A1l, B1h, B1l, KP, 0, 0, nullptr, nullptr)))
+        return rc;
+    if ((rc = make_problem(ctx, q[1], (float2*)C2, 0, M, N2, A2h, A2l, B2h, B2l, KP, 0, 0, nullptr, nullptr)))
+        return rc;
+    q[0].p.ldc = ldc1;
+    q[1].p.ldc = ldc2;
+    q[0].p.nfast = q[1].p.nfast = 1;
+    return launch_gemm(ctx, st, q, 2, KP, 0, nullptr);
 }
 
 // ---- the no-pivot LU's block column in three launches (see lu_nopiv.cu)

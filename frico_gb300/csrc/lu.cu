@@ -27,7 +27,6 @@ namespace frico {
 
 static const int kNB = 64;          // LU block width
 static const int kMaxPanelCTAs = 1024;
-static const long long kBarrierTimeoutCycles = 4000000000LL;  // ~2 s at 2 GHz
 
 template <typename R> struct PanelWS {
     unsigned* bar;        // [0] count, [1] generation
@@ -40,7 +39,7 @@ template <typename R> struct PanelWS {
 // Grid-wide barrier for a cooperative launch. The wait is bounded: on timeout
 // the CTA records FRICO_DEV_ERR_TIMEOUT and returns false, so a lost CTA turns
 // into an error status instead of a hung GPU.
-__device__ bool grid_barrier(unsigned* bar, DeviceStatus* st, int where) {
+__device__ bool grid_barrier(unsigned* bar, DeviceStatus* st, int where, long long lim) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -56,7 +55,7 @@ __device__ bool grid_barrier(unsigned* bar, DeviceStatus* st, int where) {
         } else {
             long long t0 = clock64();
             while (*vgen == gen) {
-                if (clock64() - t0 > kBarrierTimeoutCycles) {
+                if (clock64() - t0 > lim) {
                     ok = 0;
                     if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = where;
                     break;
@@ -109,7 +108,7 @@ __device__ void block_argmax(const cplx<R>* col, int rs, int nr, R* out_val, int
 template <typename R>
 __global__ void __launch_bounds__(256) k_panel(cplx<R>* A, int64_t lda, int n, int k0, int jb,
                                               int rows_per, int32_t* ipiv, PanelWS<R> ws,
-                                              DeviceStatus* st) {
+                                              DeviceStatus* st, long long lim) {
     using C = cplx<R>;
     extern __shared__ __align__(16) unsigned char smraw[];
     C* sm = (C*)smraw;             // [jb][rows_per]
@@ -143,7 +142,7 @@ __global__ void __launch_bounds__(256) k_panel(cplx<R>* A, int64_t lda, int n, i
     };
 
     publish(0, 0);
-    if (!grid_barrier(ws.bar, st, k0)) return;
+    if (!grid_barrier(ws.bar, st, k0, lim)) return;
 
     for (int c = 0; c < jb; c++) {
         const int k = k0 + c, par = c & 1;
@@ -198,7 +197,7 @@ __global__ void __launch_bounds__(256) k_panel(cplx<R>* A, int64_t lda, int n, i
         __syncthreads();
         if (c + 1 < jb) {
             publish(c + 1, par ^ 1);
-            if (!grid_barrier(ws.bar, st, k + 1)) return;
+            if (!grid_barrier(ws.bar, st, k + 1, lim)) return;
         }
     }
     for (int idx = tid; idx < nr * jb; idx += blockDim.x) {
@@ -815,7 +814,8 @@ template <typename R> struct LuDriver {
         int n_ = n, k0_ = k0, w_ = w, rp_ = rows_per;
         PanelWS<R> ws_ = ws;
         DeviceStatus* dst_ = dst;
-        void* args[] = {&A, &lda_, &n_, &k0_, &w_, &rp_, &ipiv, &ws_, &dst_};
+        long long lim = wait_limit(ctx);
+        void* args[] = {&A, &lda_, &n_, &k0_, &w_, &rp_, &ipiv, &ws_, &dst_, &lim};
         count_launch(ctx);
         return cuda_check(ctx, cudaLaunchCooperativeKernel((void*)k_panel<R>, dim3(G), dim3(256), args, smem, st),
                           "k_panel");

@@ -21,7 +21,6 @@ namespace frico {
 
 static const int kB = 64;        // block rows
 static const int kRc = 8;        // right-hand sides per pass
-static const long long kWaitCycles = 4000000000LL;
 
 // One CTA per diagonal block: Linv = L_bb^{-1} (unit lower), Uinv = U_bb^{-1}.
 // Thread j owns column j of the inverse (forward / backward substitution
@@ -80,7 +79,7 @@ __global__ void __launch_bounds__(128) k_invert_diag(const C* __restrict__ LU, i
 template <typename C, bool LOWER, int NC>
 __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, int64_t lda, int n, const C* __restrict__ Dinv,
                                                    C* W, int64_t ldw, int nrhs, int* flags, unsigned* ticket, int epoch,
-                                                   DeviceStatus* st) {
+                                                   DeviceStatus* st, long long lim) {
     using R = decltype(W[0].x);
     __shared__ C xs[2][kB][kRc];         // published blocks y_c (double buffer)
     __shared__ C part[4][kB][kRc];       // partial sums of the 4 column groups
@@ -134,7 +133,7 @@ __global__ void __launch_bounds__(256) k_trsv_chain(const C* __restrict__ LU, in
                 long long t0 = clock64();
                 while (*f != epoch) {
                     if (*e) { s_abort = 1; break; }
-                    if (clock64() - t0 > kWaitCycles) {
+                    if (clock64() - t0 > lim) {
                         if (atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
                         s_abort = 1;
                         break;
@@ -277,7 +276,8 @@ template <bool LOWER, int NC>
 __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict__ LU, int64_t lda, int n,
                                                       const float2* __restrict__ Dinv, const float2* __restrict__ M,
                                                       const float2* __restrict__ Win, int64_t ldin, float2* Xout,
-                                                      int64_t ldout, int nrhs, unsigned* ticket, DeviceStatus* st) {
+                                                      int64_t ldout, int nrhs, unsigned* ticket, DeviceStatus* st,
+                                                      long long lim) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* Ds = (float2*)smraw;                                                  // [c * 128 + r]
     float2 (*xs)[kB2][kRc] = reinterpret_cast<float2 (*)[kB2][kRc]>(Ds + kB2 * kB2);   // [2]
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
                     xs[buf][rr][c] = v;
                 }
                 if (!__any_sync(0xffffffffu, pending)) break;
-                if (lane == 0 && (*e || clock64() - t0 > kWaitCycles)) {
+                if (lane == 0 && (*e || clock64() - t0 > lim)) {
                     if (!*e && atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT) == 0) st->where = cb;
                     s_abort = 1;
                 }
@@ -420,24 +420,24 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
 // ------------------------------------------------------------------ host side
 template <typename C, bool LOWER>
 static void launch_chain_nc(int nc, int nb, cudaStream_t st, const C* LU, int n, const C* D, C* W, int64_t ldw,
-                            int* flags, unsigned* ticket, int epoch, DeviceStatus* dst) {
+                            int* flags, unsigned* ticket, int epoch, DeviceStatus* dst, long long lim) {
     if (nc == 1)
-        k_trsv_chain<C, LOWER, 1><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+        k_trsv_chain<C, LOWER, 1><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst, lim);
     else if (nc == 2)
-        k_trsv_chain<C, LOWER, 2><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+        k_trsv_chain<C, LOWER, 2><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst, lim);
     else if (nc <= 4)
-        k_trsv_chain<C, LOWER, 4><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+        k_trsv_chain<C, LOWER, 4><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst, lim);
     else
-        k_trsv_chain<C, LOWER, kRc><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst);
+        k_trsv_chain<C, LOWER, kRc><<<nb, 256, 0, st>>>(LU, n, n, D, W, ldw, nc, flags, ticket, epoch, dst, lim);
 }
 
 template <typename C>
 static void launch_chain(bool lower, int nc, int nb, cudaStream_t st, const C* LU, int n, const C* D, C* W,
-                         int64_t ldw, int* flags, unsigned* ticket, int epoch, DeviceStatus* dst) {
+                         int64_t ldw, int* flags, unsigned* ticket, int epoch, DeviceStatus* dst, long long lim) {
     if (lower)
-        launch_chain_nc<C, true>(nc, nb, st, LU, n, D, W, ldw, flags, ticket, epoch, dst);
+        launch_chain_nc<C, true>(nc, nb, st, LU, n, D, W, ldw, flags, ticket, epoch, dst, lim);
     else
-        launch_chain_nc<C, false>(nc, nb, st, LU, n, D, W, ldw, flags, ticket, epoch, dst);
+        launch_chain_nc<C, false>(nc, nb, st, LU, n, D, W, ldw, flags, ticket, epoch, dst, lim);
 }
 
 struct TrsvWs {
@@ -473,13 +473,15 @@ int trsv_solve(frico_gpu_ctx* ctx, const C* LU, DevBuf& ws_buf, DevBuf& flag_buf
     unsigned* ticket = (unsigned*)(flags + nb + 32);
     DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
     int rc;
+    // a wait that gave up in an earlier solve must not end this one's kernels
+    if ((rc = cuda_check(ctx, cudaMemsetAsync(&dst->err, 0, sizeof(int), ctx->stream), "status"))) return rc;
     for (int c0 = 0; c0 < nrhs; c0 += kRc) {
         int nc = std::min(kRc, nrhs - c0);
         for (int pass = 0; pass < 2; pass++) {
             int epoch = ++ctx->trsv_epoch;
             if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream), "ticket"))) return rc;
             launch_chain<C>(pass == 0, nc, nb, ctx->stream, LU, n, pass == 0 ? Linv : Uinv, W + c0 * ldw, ldw, flags,
-                            ticket, epoch, dst);
+                            ticket, epoch, dst, wait_limit(ctx));
             count_launch(ctx);
         }
     }
@@ -534,16 +536,16 @@ int trsv128_prepare(frico_gpu_ctx* ctx, cudaStream_t st) {
 template <bool LOWER>
 static void launch_chain128(int nc, int nb, cudaStream_t st, const float2* LU, int n, const float2* D,
                             const float2* M, const float2* Win, int64_t ldin, float2* Xout, int64_t ldout,
-                            unsigned* ticket, DeviceStatus* dst) {
+                            unsigned* ticket, DeviceStatus* dst, long long lim) {
     if (nc == 1)
-        k_trsv_chain128<LOWER, 1><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst);
+        k_trsv_chain128<LOWER, 1><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst, lim);
     else if (nc == 2)
-        k_trsv_chain128<LOWER, 2><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst);
+        k_trsv_chain128<LOWER, 2><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst, lim);
     else if (nc <= 4)
-        k_trsv_chain128<LOWER, 4><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst);
+        k_trsv_chain128<LOWER, 4><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket, dst, lim);
     else
         k_trsv_chain128<LOWER, kRc><<<nb, 512, kChain128Smem, st>>>(LU, n, n, D, M, Win, ldin, Xout, ldout, nc, ticket,
-                                                                     dst);
+                                                                     dst, lim);
 }
 
 // Lower pass W -> X (scratch), upper pass X -> W; each output pre-filled with the pattern.
@@ -557,6 +559,7 @@ static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     const float2* Uinv = Linv + size_t(nb) * kB2 * kB2;
     const float2* Mlow = Linv + size_t(2) * nb * kB2 * kB2;
     const float2* Mup = Linv + size_t(3) * nb * kB2 * kB2;
+    const long long lim = wait_limit(ctx);
     cudaStream_t st = ctx->stream;
     int rc = device_once(ctx, kOnceTrsv128, [](frico_gpu_ctx* c) {
         const void* fns[8] = {(const void*)k_trsv_chain128<true, 1>,   (const void*)k_trsv_chain128<true, 2>,
@@ -572,18 +575,19 @@ static int trsv128_solve(frico_gpu_ctx* ctx, float2* W, int nrhs, int64_t ldw) {
     });
     if (rc) return rc;
     if ((rc = ensure(ctx, ctx->trsv_x, sizeof(float2) * size_t(n) * kRc))) return rc;
+    if ((rc = cuda_check(ctx, cudaMemsetAsync(&dst->err, 0, sizeof(int), st), "status"))) return rc;
     float2* X = (float2*)ctx->trsv_x.p;
     for (int c0 = 0; c0 < nrhs; c0 += kRc) {
         const int nc = std::min(kRc, nrhs - c0);
         float2* Wc = W + c0 * ldw;
         if ((rc = cuda_check(ctx, cudaMemsetAsync(X, 0xFF, sizeof(float2) * size_t(n) * nc, st), "unset x"))) return rc;
         if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "ticket"))) return rc;
-        launch_chain128<true>(nc, nb, st, LU, n, Linv, Mlow, Wc, ldw, X, n, ticket, dst);
+        launch_chain128<true>(nc, nb, st, LU, n, Linv, Mlow, Wc, ldw, X, n, ticket, dst, lim);
         if ((rc = cuda_check(ctx, cudaMemset2DAsync(Wc, sizeof(float2) * ldw, 0xFF, sizeof(float2) * n, nc, st),
                              "unset w")))
             return rc;
         if ((rc = cuda_check(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "ticket"))) return rc;
-        launch_chain128<false>(nc, nb, st, LU, n, Uinv, Mup, X, n, Wc, ldw, ticket, dst);
+        launch_chain128<false>(nc, nb, st, LU, n, Uinv, Mup, X, n, Wc, ldw, ticket, dst, lim);
         count_launch(ctx, 2);
     }
     return cuda_check(ctx, cudaGetLastError(), "k_trsv_chain128");

@@ -108,7 +108,7 @@ class Simulation:
                  h_phase: str = "compat", edge_length: str = "xy", device: int = 0,
                  max_refine_iters: int = 30, refine_tol: float = 1e-12, profile_kernels: bool = False,
                  gemm_engine: str = "auto", pivoting: str = "auto", refine: str = "auto",
-                 residual: str = "auto"):
+                 residual: str = "auto", wait_limit_cycles: int = 0, fields: str = "auto"):
         self.lib = _abi.load()
         self.mesh = mesh
         self.fs = make_function_space(mesh, edge_length)
@@ -121,7 +121,10 @@ class Simulation:
                                 {"auto": _abi.PIVOT_AUTO, "partial": _abi.PIVOT_PARTIAL,
                                  "none": _abi.PIVOT_NONE}[pivoting],
                                 {"auto": _abi.REFINE_AUTO, "classic": _abi.REFINE_CLASSIC}[refine],
-                                {"auto": _abi.RESIDUAL_AUTO, "fp64": _abi.RESIDUAL_FP64}[residual])
+                                {"auto": _abi.RESIDUAL_AUTO, "fp64": _abi.RESIDUAL_FP64}[residual],
+                                int(wait_limit_cycles),
+                                {"auto": _abi.FIELDS_AUTO, "direct": _abi.FIELDS_DIRECT,
+                                 "gemm": _abi.FIELDS_GEMM}[fields])
         self.ctx = C.c_void_p()
         rc = self.lib.frico_gpu_ctx_create(C.byref(self.ctx), device, C.byref(self.opt))
         _check(self.lib, rc, what="frico_gpu_ctx_create (is a CUDA device visible?)")
@@ -172,13 +175,16 @@ class Simulation:
         self.freq = float(freq)
         return Z
 
-    def set_matrix(self, Z: np.ndarray):
-        """A Z assembled elsewhere (n x n complex) in place of compute_matrix; solve()
-        then factors it, as FRICO's solve_general takes its matrix argument."""
+    def set_matrix(self, Z: np.ndarray, freq: float):
+        """A Z assembled elsewhere (n x n complex, at `freq` Hz) in place of
+        compute_matrix; solve() then factors it, as FRICO's solve_general takes its
+        matrix argument. With approx_matrix or force_symmetry only the upper
+        triangle is used (solve_symmetric's zsytrf with uplo = 'U')."""
         Zf = np.asarray(Z, np.complex128, order="F")
         if Zf.shape != (self.n, self.n):
             raise ValueError(f"set_matrix: Z must be {self.n} x {self.n}")
-        self._call("frico_gpu_set_matrix", ptr(Zf), self.n)
+        self._call("frico_gpu_set_matrix", float(freq), ptr(Zf), self.n)
+        self.freq = float(freq)
 
     def set_nrhs(self, nrhs: int):
         self._call("frico_gpu_set_nrhs", int(nrhs))

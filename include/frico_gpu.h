@@ -91,7 +91,19 @@ typedef struct frico_gpu_options {
     int32_t pivoting;        /* FRICO_PIVOT_* (mixed precision only; FP64 always pivots) */
     int32_t refine_mode;     /* FRICO_REFINE_* (mixed precision only)        */
     int32_t residual_mode;   /* FRICO_RESIDUAL_* (mixed precision refinement) */
+    int64_t wait_limit_cycles;/* limit, in SM clock cycles, of every device-side wait on another
+                                 CTA (chained triangular solves, the pivoted panel's grid
+                                 barrier); <= 0: 4e9 (about 2 s). A wait that runs out ends its
+                                 kernel, which returns FRICO_GPU_ETIMEOUT; the context stays
+                                 usable. The tensor-core GEMM waits only on its own TMA copies
+                                 and MMAs and keeps its fixed limit of 4e9 cycles. */
+    int32_t fields_engine;   /* FRICO_FIELDS_*: E of many right-hand sides (eval_fields_multi) */
 } frico_gpu_options;
+
+#define FRICO_FIELDS_AUTO   0  /* mixed precision: E of >= 4 columns as tensor-core GEMMs (tcgen05 3xTF32,
+                                  FP64 phase and sums); FP64 precision and H: the direct kernels */
+#define FRICO_FIELDS_DIRECT 1  /* direct (point, triangle) kernels: FP64, or double-float for mixed */
+#define FRICO_FIELDS_GEMM   2  /* E as tensor-core GEMMs whatever the precision (error if unavailable) */
 
 #define FRICO_REFINE_AUTO    0  /* classical refinement, GMRES (max(120, 2 x max_refine_iters) iterations) when it contracts slowly */
 #define FRICO_REFINE_CLASSIC 1  /* classical refinement only                                           */
@@ -190,8 +202,15 @@ int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out, int64_t l
  * (src/lapack_wrappers.h:10-19) for a Z the caller assembled itself: upload the
  * n x n complex matrix (column-major, leading dim ldz >= n, n = the mesh's RWG
  * count) in place of a fill; the next frico_gpu_solve factors it (for
- * FRICO_PREC_MIXED, a complex64 copy refined against this FP64 Z). */
-int frico_gpu_set_matrix(frico_gpu_ctx* ctx, const frico_c128* Z, int64_t ldz);
+ * FRICO_PREC_MIXED, a complex64 copy refined against this FP64 Z).
+ * freq (Hz, > 0) is the frequency Z belongs to, as freq_context::frequency
+ * holds it beside Z (src/emw_solver.h:57-75): lumping and field evaluation of
+ * the solution use it.
+ * With approx or force_symmetry set, FRICO solves with solve_symmetric
+ * (zsytrf/zsytrs, uplo = 'U', src/lapack_wrappers.cpp:135-177), which reads
+ * only the upper triangle of A: the lower triangle is then taken as the
+ * transpose of the upper one, so a non-symmetric Z gives FRICO's answer. */
+int frico_gpu_set_matrix(frico_gpu_ctx* ctx, double freq, const frico_c128* Z, int64_t ldz);
 
 /* Set the right-hand-side count (columns of V); resets V to zero. */
 int frico_gpu_set_nrhs(frico_gpu_ctx* ctx, int32_t nrhs);
@@ -235,7 +254,10 @@ int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t npts, const d
  * a post-processing loop that must not pay cudaMalloc's device-wide
  * synchronisation. P_dev[3*npts] (points), E_dev[3*npts], H_dev[3*npts]
  * (row-major rows of 3; either may be NULL) are device memory of the
- * context's device; anything else is EINVAL. npts <= 43690: the partial sums
+ * context's device; anything else is EINVAL. The kernels store E and H as
+ * 16-byte complex values and read P as doubles: E_dev and H_dev must be
+ * 16-byte aligned and P_dev 8-byte aligned, else EINVAL (checked before any
+ * launch, so a misaligned view never reaches the GPU). npts <= 43690: the partial sums
  * use one fixed 4 MiB device array per device, and larger npts is EINVAL.
  * The currents of `col` must already be lumped (frico_gpu_lump_currents),
  * else ESTATE. The kernels are queued on the context stream and the call
@@ -243,7 +265,9 @@ int frico_gpu_eval_fields(frico_gpu_ctx* ctx, int32_t col, int64_t npts, const d
  * them. The scratch array is shared by every context on the device, so calls
  * whose kernels overlap on the GPU race. The first call on each device looks
  * up the scratch address (which may load the library's device code): make
- * it before any stream capture. */
+ * it before any stream capture. That address is cached per device for the
+ * life of the process: after cudaDeviceReset on a device the cache is stale,
+ * so do not call this entry point again in that process. */
 int frico_gpu_eval_fields_noalloc(frico_gpu_ctx* ctx, int32_t col, int64_t npts,
                                   const double* P_dev, frico_c128* E_dev, frico_c128* H_dev);
 
@@ -325,7 +349,11 @@ int frico_gpu_adjoint(frico_gpu_ctx* ctx, double freq, int32_t n_itf, const int3
 
 /* eval_fields for RHS columns [col0, col0 + ncols) at the same npts points:
  * E[ncols][npts][3], H[ncols][npts][3] (either may be NULL). One pass over
- * (point, triangle) pairs serves every column (the Green function is shared). */
+ * (point, triangle) pairs serves every column (the Green function is shared).
+ * With fields_engine selecting GEMMs (and H not asked for), E comes from two
+ * complex matrix products over the triangles on the tensor cores: the Green
+ * function with the point's phase e^{-jk|P|} factored out, times the lumped
+ * currents (accurate to ~1e-7 of |E|, against ~1e-12 for the direct kernels). */
 int frico_gpu_eval_fields_multi(frico_gpu_ctx* ctx, int32_t col0, int32_t ncols, int64_t npts,
                                 const double* P, frico_c128* E, frico_c128* H);
 /* bistatic_RCS_unit_Ei at sph2rect(R, theta[i], phi[i]) for every column:
@@ -349,14 +377,6 @@ int frico_gpu_rcs_points(frico_gpu_ctx* ctx, int32_t col, double R, int64_t npts
                          const double* theta, const double* phi, double* out);
 
 int frico_gpu_last_stats(frico_gpu_ctx* ctx, frico_gpu_stats* stats);
-
-/* Diagnostic: C -= A B with the LU's complex64 trailing-update kernel
- * (engine FRICO_GEMM_SIMT, FRICO_GEMM_TC: 3xTF32 operands, or
- * FRICO_GEMM_TC_F16: 3xFP16 operands); A m x k (ld m), B k x n (ld k),
- * C m x n (ld m), column-major host buffers. No FRICO counterpart: it exposes
- * one internal kernel so that it can be tested on its own. */
-int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, int32_t k, const frico_c64* A,
-                          const frico_c64* B, frico_c64* C, int32_t engine);
 
 #ifdef __cplusplus
 }

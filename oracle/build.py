@@ -38,15 +38,23 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
-def reference_dir() -> Path:
-    """The FRICO checkout whose sources pin the oracle (FRICO_REFERENCE overrides)."""
-    return Path(os.environ.get("FRICO_REFERENCE", "/root/reference"))
+# Where this build recipe looks for the FRICO checkout when FRICO_REFERENCE is unset:
+# the read-only mount of the build machine. Machines without it (the GPU hosts) skip
+# the reference build and use the committed fixtures.
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_dir() -> Path | None:
+    """The FRICO checkout whose sources pin the oracle: $FRICO_REFERENCE, else the
+    build machine's mount; None when neither holds FRICO's sources."""
+    ref = Path(os.environ.get("FRICO_REFERENCE") or DEFAULT_REFERENCE)
+    return ref if (ref / "src" / "quadratures.cpp").exists() else None
 
 
 def build_ref() -> Path | None:
     """Compile FRICO's own sources (where they lie) into oracle/_ref/, if present."""
     ref = reference_dir()
-    if not (ref / "src" / "quadratures.cpp").exists() or not (HERE / "ref" / "Makefile").exists():
+    if ref is None or not (HERE / "ref" / "Makefile").exists():
         return None
     r = subprocess.run(["make", "-s", "-C", str(HERE / "ref"), f"REF={ref}"], capture_output=True, text=True)
     if r.returncode != 0:

@@ -344,6 +344,51 @@ void oracle_compute_matrix_cols(void* sp, double freq, int64_t c0, int64_t c1, d
     }
 }
 
+// Conditioning of each entry of compute_matrix (columns [c0, c1)): the sum of the
+// magnitudes of the terms the entry's double loop adds, sum |prodl w (v - sv) g|
+// over the four blocks and their quadrature pairs (same loops as above). Where the
+// blocks cancel, FP64 evaluations of an entry in different orders can only agree
+// to a few ulps of this sum, not of the entry itself. Mout column-major, n x (c1 - c0).
+void oracle_compute_matrix_magnitudes(void* sp, double freq, int64_t c0, int64_t c1, double* Mout) {
+    State* s = (State*)sp;
+    const Mesh& msh = s->msh;
+    const int64_t n = int64_t(msh.bfs.size());
+    double omega = 2.0 * M_PI * freq;
+    double inv_ksq = 1. / (omega * omega * MU0 * EPS0);
+    const size_t deg = s->degree;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t ii = c0; ii < c1; ii++) {
+        const Bf& ibf = msh.bfs[ii];
+        auto iqps_minus = msh.integrate(ibf.itminus, deg);
+        auto iqps_plus = msh.integrate(ibf.itplus, deg);
+        for (int64_t jj = 0; jj < n; jj++) {
+            const Bf& jbf = msh.bfs[jj];
+            bool split_minus = (jbf.itminus == ibf.itminus) || (jbf.itminus == ibf.itplus);
+            bool split_plus = (jbf.itplus == ibf.itminus) || (jbf.itplus == ibf.itplus);
+            auto jqps_minus = split_minus ? msh.integrate_subtri(jbf.itminus, deg) : msh.integrate(jbf.itminus, deg);
+            auto jqps_plus = split_plus ? msh.integrate_subtri(jbf.itplus, deg) : msh.integrate(jbf.itplus, deg);
+            double mag = 0.0;
+            double prodl = 0.25 * ibf.length * jbf.length * M_1_PI;
+            auto block = [&](const std::vector<qpoint>& I, const std::vector<qpoint>& J, bool im, bool jm,
+                             double inv_AA) {
+                for (const auto& iqp : I)
+                    for (const auto& jqp : J) {
+                        double v = 0.25 * dot(im ? ibf.rho_minus(iqp.p) : ibf.rho_plus(iqp.p),
+                                              jm ? jbf.rho_minus(jqp.p) : jbf.rho_plus(jqp.p));
+                        double w = iqp.w * jqp.w * inv_AA;
+                        double Rij = norm(iqp.p - jqp.p);
+                        mag += std::abs(prodl * w * (v - inv_ksq)) / Rij;
+                    }
+            };
+            block(iqps_minus, jqps_minus, true, true, 1. / (ibf.Aminus * jbf.Aminus));
+            block(iqps_minus, jqps_plus, true, false, 1. / (ibf.Aminus * jbf.Aplus));
+            block(iqps_plus, jqps_minus, false, true, 1. / (ibf.Aplus * jbf.Aminus));
+            block(iqps_plus, jqps_plus, false, false, 1. / (ibf.Aplus * jbf.Aplus));
+            Mout[jbf.matrix_index + (ibf.matrix_index - c0) * n] = mag;
+        }
+    }
+}
+
 void oracle_compute_matrix(void* sp, double freq, double* Zout) {
     oracle_compute_matrix_cols(sp, freq, 0, int64_t(((State*)sp)->msh.bfs.size()), Zout);
 }

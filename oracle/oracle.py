@@ -39,6 +39,7 @@ def _load():
             "oracle_dunavant": ([i32, vp, vp, vp, vp], i32),
             "oracle_compute_matrix": ([vp, d, vp], None),
             "oracle_compute_matrix_cols": ([vp, d, i64, i64, vp], None),
+            "oracle_compute_matrix_magnitudes": ([vp, d, i64, i64, vp], None),
             "oracle_compute_matrix_approx": ([vp, d, vp], None),
             "oracle_reorient": ([vp, i32, vp, i32, vp], i32),
             "oracle_rhs_delta_gap": ([vp, d, i32, vp, d, d, vp, vp], None),
@@ -111,6 +112,16 @@ class Oracle:
         Z = np.zeros((self.n, c1 - c0), np.complex128, order="F")
         self.lib.oracle_compute_matrix_cols(self.s, float(freq), int(c0), int(c1), _p(Z))
         return Z
+
+    def compute_matrix_magnitudes(self, freq: float, c0: int = 0, c1: int | None = None) -> np.ndarray:
+        """Columns [c0, c1) of M: M[j, i] = sum of the magnitudes of the terms that
+        compute_matrix adds into Z[j, i] (quadrature mode). M / |Z| is the entry's
+        cancellation factor; FP64 evaluations of Z[j, i] in different summation
+        orders agree to a few ulps of M[j, i]."""
+        c1 = self.n if c1 is None else c1
+        M = np.zeros((self.n, c1 - c0), order="F")
+        self.lib.oracle_compute_matrix_magnitudes(self.s, float(freq), int(c0), int(c1), _p(M))
+        return M
 
     def reorient(self, tags, force: bool = False):
         t = np.asarray(tags, np.int32)

@@ -99,3 +99,75 @@ def test_adjoint_rejects_unsupported_fill(gpu_lib):
         sim.adjoint(FREQ, FEED, P_OBS)
     assert e.value.code == -1
     sim.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# The adjoint-sensitivity configuration: bowtie N ~ 3000 at 500 MHz, 64 seeded random unit
+# directions over all vertex coordinates, central differences of the FP64 path with step
+# 1e-6 wavelength.
+#
+# What the differences can resolve: the FP64 forward path reproduces Zin and |E|^2 only to
+# about 1e-10 of their values when the geometry moves (kappa_1(Z) = 3e8 at 500 MHz amplifies the
+# fill's rounding, in FRICO's summation order as in this one), so a central difference with step
+# h carries a noise of about nu / h, nu the forward path's reproducibility. nu is measured here,
+# not assumed: the forward path on copies of the mesh with the vertex list permuted (the same
+# geometry, different edge order, so different rounding everywhere) differs from the original by
+# nu_k in objective k. Each direction must satisfy |adjoint - FD| <= 1e-5 |FD| + 4 nu_k / h; for
+# Re / Im Zin that is the 1e-5 relative bound wherever |FD| is above the noise floor 4e5 nu_k / h.
+FREQ_CFG = 500e6
+
+
+def _permuted(mesh, seed):
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(mesh.vertices.shape[0])
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(perm.size)
+    m = meshes.bowtie(*meshes.BOWTIE_PRESETS[3000])
+    m.vertices = mesh.vertices[perm]
+    m.triangles = inv[mesh.triangles]
+    m.curves = inv[np.asarray(mesh.curves)] if len(mesh.curves) else mesh.curves
+    return m
+
+
+@pytest.mark.gpu
+def test_adjoint_bowtie_3000_against_central_differences(gpu_lib):
+    nx, ny = meshes.BOWTIE_PRESETS[3000]
+    mesh = meshes.bowtie(nx, ny)
+    sim = Simulation(mesh, precision="fp64")
+    assert 2900 <= sim.n <= 3100
+    out = sim.adjoint(FREQ_CFG, FEED, P_OBS)
+    sim.close()
+    G = np.stack([out["grad_zin_re"], out["grad_zin_im"], out["grad_e2"]])
+    f0 = _forward(mesh, FREQ_CFG)
+    nu = np.max([np.abs(_forward(_permuted(mesh, s), FREQ_CFG) - f0) for s in (1, 2, 3)], axis=0)
+    assert np.all(nu <= 1e-9 * np.abs(f0)), nu
+    h = 1e-6 * C0 / FREQ_CFG
+    m = meshes.bowtie(nx, ny)
+    rng = np.random.default_rng(20260104)
+    strict = 0
+    for _ in range(64):
+        d = rng.standard_normal(mesh.vertices.shape)
+        d /= np.linalg.norm(d)
+        m.vertices = mesh.vertices + h * d
+        fp = _forward(m, FREQ_CFG)
+        m.vertices = mesh.vertices - h * d
+        fm = _forward(m, FREQ_CFG)
+        fd = (fp - fm) / (2 * h)
+        ad = np.einsum("kvc,vc->k", G, d)
+        assert np.all(np.abs(ad - fd) <= 1e-5 * np.abs(fd) + 4 * nu / h), (ad, fd, nu / h)
+        strict += int(np.all(np.abs(ad[:2] - fd[:2]) <= 1e-5 * np.abs(fd[:2])))
+    print(f"N={mesh.nt} triangles: Zin gradients within 1e-5 relative of FD in {strict}/64 directions; "
+          f"noise floor nu/h = {nu / h}")
+
+
+@pytest.mark.gpu
+def test_adjoint_bowtie_3000_mixed_matches_fp64(gpu_lib):
+    mesh = meshes.bowtie(*meshes.BOWTIE_PRESETS[3000])
+    res = {}
+    for precision in ("fp64", "mixed"):
+        sim = Simulation(mesh, precision=precision)
+        res[precision] = sim.adjoint(FREQ_CFG, FEED, P_OBS)
+        sim.close()
+    for k in ("grad_zin_re", "grad_zin_im", "grad_e2"):
+        assert np.linalg.norm(res["mixed"][k] - res["fp64"][k]) <= 1e-6 * np.linalg.norm(res["fp64"][k]), k
+    assert abs(res["mixed"]["zin"] - res["fp64"]["zin"]) <= 1e-8 * abs(res["fp64"]["zin"])

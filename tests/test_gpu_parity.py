@@ -327,12 +327,55 @@ def test_set_matrix_solves_a_given_z(gpu_lib, sphere2, precision):
     Xr = np.linalg.solve(Zr, B)
     tol = OUT_TOL if precision == "fp64" else MIXED_TOL
     sim = Simulation(sphere2, precision=precision)
-    sim.set_matrix(Zr)
+    sim.set_matrix(Zr, f)
     sim.set_rhs(B)
     assert rel_norm(sim.solve(), Xr) < tol
-    sim.set_matrix(2.0 * Zr)
+    sim.set_matrix(2.0 * Zr, f)
     sim.set_rhs(B)
     assert rel_norm(sim.solve(), 0.5 * Xr) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_set_matrix_fields_use_its_frequency(gpu_lib, sphere2, precision):
+    """Fields after frico_gpu_set_matrix are evaluated at the frequency given with
+    Z, as after a fill at that frequency (the lumping and the Green function of
+    eval_fields take it from the context), even after a fill at another one."""
+    f = 450e6
+    pw = PlaneWave(0.0, 0.0, 1.0, 0.0)
+    pts = meshes.sph2rect(10.0, np.linspace(0.0, np.pi, 19), np.zeros(19))
+    ref = Simulation(sphere2, precision=precision)
+    ref.compute_matrix(f)
+    ref.update_rhs(f, pw)
+    ref.solve()
+    E_ref, H_ref = ref.eval_fields(pts)
+    o = oracle_for(sphere2)
+    sim = Simulation(sphere2, precision=precision)
+    sim.compute_matrix(300e6)            # a fill at another frequency first
+    sim.set_matrix(o.compute_matrix(f), f)
+    sim.update_rhs(f, pw)
+    sim.solve()
+    E, H = sim.eval_fields(pts)
+    tol = OUT_TOL if precision == "fp64" else MIXED_TOL
+    assert rel_norm(E, E_ref) < tol and rel_norm(H, H_ref) < tol
+
+
+def test_set_matrix_symmetric_modes_read_the_upper_triangle(gpu_lib, sphere2):
+    """With force_symmetry (FRICO's -S: solve_symmetric, zsytrf uplo = 'U') the
+    matrix argument's lower triangle is not read: a Z whose lower triangle is
+    garbage solves as the symmetric matrix built from its upper triangle."""
+    f = 450e6
+    o = oracle_for(sphere2)
+    Zr = o.compute_matrix(f)
+    Zs = np.triu(Zr) + np.triu(Zr, 1).T
+    rng = np.random.default_rng(5)
+    B = rng.standard_normal((o.n, 2)) + 1j * rng.standard_normal((o.n, 2))
+    Xr = np.linalg.solve(Zs, B)
+    Zbad = Zr.copy()
+    Zbad[np.tril_indices(o.n, -1)] = 1e3 * (1 + 1j)
+    sim = Simulation(sphere2, precision="fp64", force_symmetry=True)
+    sim.set_matrix(Zbad, f)
+    sim.set_rhs(B)
+    assert rel_norm(sim.solve(), Xr) < OUT_TOL
 
 
 def test_sphere_l4_mixed_matches_fp64_at_full_size(gpu_lib):

@@ -178,3 +178,32 @@ def test_oracle_dunavant_exactness():
                 exact = math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
             got = np.sum(q[:, 3] * q[:, 0] ** a * q[:, 1] ** b)
             assert abs(got - exact) < 1e-11, (d, a, b, got, exact)
+
+
+def test_abi_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the C-ABI's structs have the sizes and field offsets
+    the C compiler gives the header's declarations."""
+    import shutil
+    import subprocess
+    from frico_gb300 import _abi
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {"frico_gpu_options": _abi.Options, "frico_gpu_stats": _abi.Stats,
+               "frico_sweep_report": _abi.SweepReport, "frico_adjoint_result": _abi.AdjointResult,
+               "frico_port_values": _abi.PortValues}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "frico_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

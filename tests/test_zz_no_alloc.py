@@ -77,6 +77,11 @@ def test_noalloc_rejects_before_launch(gpu_lib):
     host = np.zeros((16, 3))
     assert _noalloc(sim, host.ctypes.data, E_dev.data_ptr(), 0, 16) == -1
     assert b"device" in sim.lib.frico_gpu_last_error(sim.ctx)
+    # misaligned views (one double past an aligned buffer) are refused before any launch
+    assert _noalloc(sim, P_dev.data_ptr(), E_dev.data_ptr() + 8, 0, 16) == -1
+    assert b"aligned" in sim.lib.frico_gpu_last_error(sim.ctx)
+    assert _noalloc(sim, P_dev.data_ptr() + 4, E_dev.data_ptr(), 0, 16) == -1
+    assert b"aligned" in sim.lib.frico_gpu_last_error(sim.ctx)
     # currents of the column not lumped: a fresh solve clears the lumped column
     sim.solve()
     assert _noalloc(sim, P_dev.data_ptr(), E_dev.data_ptr(), 0, 16) == -6
