@@ -111,6 +111,7 @@ PROTOTYPES = {
     "frico_gpu_last_stats": [P, P],
     "frico_gpu_debug_cgemm": [P, I32, I32, I32, P, P, P, I32],
     "frico_gpu_debug_z64": [P, P, P],
+    "frico_gpu_debug_fields_gemm_config": [I32, I32],
 }
 
 _lib = None

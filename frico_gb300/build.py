@@ -23,7 +23,7 @@ LIB = LIBDIR / "libfrico_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["api.cu", "fill.cu", "lu.cu", "trsv.cu", "gemm_tc.cu", "lu_nopiv.cu", "fields.cu", "fields_multi.cu", "sweep.cu", "adjoint.cu", "gmres.cu", "fields_gemm.cu", "diag_blocked.cu",
+SOURCES = ["api.cu", "fill.cu", "lu.cu", "trsv.cu", "gemm_tc.cu", "lu_nopiv.cu", "fields.cu", "fields_multi.cu", "sweep.cu", "adjoint.cu", "gmres.cu", "fields_gemm.cu",
            "mesh_host.cpp"]
 
 

@@ -147,7 +147,7 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->xyz,     &ctx->tri,      &ctx->trigeo,   &ctx->qp,        &ctx->qps,     &ctx->rwg_itm,
                       &ctx->rwg_itp, &ctx->rwg_len,  &ctx->rwg_am,   &ctx->rwg_ap,    &ctx->rwg_vm,  &ctx->rwg_vp,
                       &ctx->rwg_itf, &ctx->tri_bf,   &ctx->tri_new,  &ctx->tri_old,   &ctx->gtab,     &ctx->smom,      &ctx->basis_aux, &ctx->z64,
-                      &ctx->z32,     &ctx->lu,       &ctx->ipiv,     &ctx->perm,      &ctx->panel_ws, &ctx->status,
+                      &ctx->z32,     &ctx->z64_keep, &ctx->res64,    &ctx->ipiv,     &ctx->perm,      &ctx->panel_ws, &ctx->status,
                       &ctx->rhs,     &ctx->sol,      &ctx->rwork,    &ctx->rwork32,   &ctx->dwork32, &ctx->norms,
                       &ctx->tri_aj,  &ctx->tri_adivj, &ctx->tri_j,   &ctx->fld_pts,   &ctx->fld_part, &ctx->fld_out,
                       &ctx->dinv,    &ctx->trsv_flags, &ctx->tc_ws,   &ctx->lut,       &ctx->dinv_t,
@@ -268,6 +268,7 @@ extern "C" int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* 
     ctx->mesh_gen++;
     ctx->geo_degree = -1;
     ctx->z_valid = ctx->factored = ctx->solved = false;
+    ctx->z64_keep_valid = false;
     ctx->lumped_col = -1;
     ctx->nrhs = 0;
     ctx->stats = frico_gpu_stats{};
@@ -289,6 +290,7 @@ extern "C" int frico_gpu_fill(frico_gpu_ctx* ctx, double freq, frico_c128* Z_out
     if (rc) return rc;
     ctx->z_valid = true;
     ctx->z32_stale = false;
+    ctx->z64_keep_valid = false;
     ctx->factored = ctx->solved = false;
     ctx->lumped_col = -1;
     if (Z_out) {
@@ -319,6 +321,7 @@ extern "C" int frico_gpu_set_matrix(frico_gpu_ctx* ctx, double freq, const frico
     ctx->freq = freq;
     ctx->z_valid = true;
     ctx->z32_stale = false;
+    ctx->z64_keep_valid = false;
     ctx->z_df = false;   // an FP64 Z as given: nothing to reassemble before an FP64 fallback
     ctx->factored = ctx->solved = false;
     ctx->lumped_col = -1;
@@ -407,6 +410,17 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
         ctx->stats.pivoting_used = partial ? FRICO_PIVOT_PARTIAL : FRICO_PIVOT_NONE;
         return r;
     };
+    // FP64 LU in place (as zgetrf), Z copied first for the refinement step of the solve
+    auto factor_fp64 = [&]() -> int {
+        const size_t zb = sizeof(double2) * size_t(ctx->n) * size_t(ctx->n);
+        int r = ensure(ctx, ctx->z64_keep, zb);
+        if (!r) r = cuda_check(ctx, cudaMemcpyAsync(ctx->z64_keep.p, ctx->z64.p, zb, cudaMemcpyDeviceToDevice, ctx->stream),
+                               "keep Z");
+        ctx->z64_keep_valid = false;
+        if (!r) r = lu_factor_fp64(ctx);
+        if (!r) ctx->z64_keep_valid = true;
+        return r;
+    };
     // factors kept: same precision, or FP64 factors a mixed solve of this Z fell back to
     const bool reuse = ctx->factored && (ctx->factor_prec == ctx->opt.precision ||
                                          (mixed && ctx->factor_prec == FRICO_PREC_FP64));
@@ -423,7 +437,7 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
             }
         } else {
             StageTimer tm(ctx, &ctx->stats.factor_ms);
-            rc = lu_factor_fp64(ctx);
+            rc = factor_fp64();
             ctx->stats.pivoting_used = FRICO_PIVOT_PARTIAL;
         }
         if (rc) {
@@ -474,7 +488,7 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
                 if ((rc = fill_matrix(ctx, ctx->freq, true))) return rc;
             }
             StageTimer tm(ctx, &ctx->stats.factor_ms);
-            rc = lu_factor_fp64(ctx);
+            rc = factor_fp64();
             if (rc) return rc;
             ctx->factor_prec = FRICO_PREC_FP64;
             ctx->z_valid = false;
@@ -498,6 +512,9 @@ extern "C" int frico_gpu_solve(frico_gpu_ctx* ctx, frico_c128* I_out, int64_t ld
             rc = cuda_check(ctx, cudaMemcpyAsync(ctx->sol.p, ctx->rhs.p, sizeof(double2) * n * ctx->nrhs,
                                                  cudaMemcpyDeviceToDevice, ctx->stream), "copy rhs");
         if (!rc) rc = lu_solve_fp64(ctx, (double2*)ctx->sol.p, ctx->nrhs, n);
+        if (!rc && ctx->z64_keep_valid)
+            rc = refine_fp64_once(ctx, (const double2*)ctx->z64_keep.p, (const double2*)ctx->rhs.p,
+                                  (double2*)ctx->sol.p);
     }
     if (rc && rc != FRICO_GPU_ENOCONV) return rc;
     ctx->solved = true;

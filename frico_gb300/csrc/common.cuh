@@ -194,7 +194,10 @@ struct frico_gpu_ctx {
     bool factored = false;
     int factor_prec = -1;         // precision of the resident factors (FP64 after a mixed fallback)
     int32_t info = 0;
-    frico::DevBuf lu, ipiv, perm, panel_ws, status;
+    frico::DevBuf z64_keep;          // FP64 drop-in: Z as it was before the in-place factorisation
+    bool z64_keep_valid = false;     // z64_keep holds the matrix of the resident FP64 factors
+    frico::DevBuf res64;             // FP64 refinement residual
+    frico::DevBuf ipiv, perm, panel_ws, status;
     int32_t nrhs = 0;
     frico::DevBuf rhs, sol, rwork, rwork32, dwork32, norms;
     frico::DevBuf dinv, trsv_flags;  // inverted diagonal blocks, chain flags + ticket
@@ -249,7 +252,7 @@ struct StageTimer {
 // the first time (device, key) is seen in this process and returns its status;
 // a failed init runs again on the next call. Safe to call from several host
 // threads (each driving its own context).
-enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceTrsv128, kOnceKeys };
+enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceTrsv128, kOnceGemmDf, kOnceKeys };
 int device_once(frico_gpu_ctx* ctx, OnceKey key, int (*init)(frico_gpu_ctx*));
 
 // Limit of the device-side waits on other CTAs (chained solves, grid barrier), in SM cycles.
@@ -269,6 +272,7 @@ int mirror_upper(frico_gpu_ctx* ctx);                         // fill.cu
 int lu_factor_fp64(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_factor_fp32(frico_gpu_ctx* ctx);                       // lu.cu
 int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb);   // lu.cu
+int refine_fp64_once(frico_gpu_ctx* ctx, const double2* Zk, const double2* B, double2* X);   // lu.cu
 int refine_solve(frico_gpu_ctx* ctx);                         // lu.cu
 int trsv_prepare_fp64(frico_gpu_ctx* ctx);                    // trsv.cu
 int trsv_prepare_fp32(frico_gpu_ctx* ctx);                    // trsv.cu
@@ -313,6 +317,10 @@ size_t tc_panel_ws_bytes(int64_t n);
 int gemm_tc_split_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, float* C1, int64_t ldc1, int N1,
                        const float* A1h, const float* A1l, const float* B1h, const float* B1l, float* C2,
                        int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
+                       const float* B2l);   // gemm_tc.cu
+int gemm_tc_dfacc_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, int group, int accumulate, double* C1,
+                       int64_t ldc1, int N1, const float* A1h, const float* A1l, const float* B1h, const float* B1l,
+                       double* C2, int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
                        const float* B2l);   // gemm_tc.cu
 bool fields_gemm_available(frico_gpu_ctx* ctx);                // fields_gemm.cu
 int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* dP, const double2* AJ,

@@ -13,10 +13,11 @@
 // G' and H' are generated per triangle chunk for all points (phase R - |P| and its
 // sine / cosine in double-float, so the phase of a 190-radian path is exact to
 // ~1e-12; the values rounded to FP32), written split into TF32 hi / lo; the
-// products run on the tcgen05 3xTF32 kernel of the LU (gemm_tc.cu) with the
-// currents as the B operand; each chunk's FP32 result is added into FP64 sums,
-// so the FP32 accumulation spans one chunk of triangles only. The point phase
-// e^{-jk|P|} and the final combination are FP64.
+// products run on the tcgen05 3xTF32 tensor cores (gemm_tc.cu, k_gemm_dfacc) with
+// the currents as the B operand; every k-step's TMEM result is moved into
+// double-float sums (the FP32 tensor-core accumulation spans 3 MMAs only), and the
+// triangle chunks add into FP64 sums. The point phase e^{-jk|P|} and the final
+// combination are FP64.
 //
 // Real-GEMM layout of the complex products (A^ real, B* doubled):
 //   A^  (points x 2 Kc):  row p = (Re G'(p, t), Im G'(p, t)) over the chunk's t
@@ -33,6 +34,7 @@
 
 #include "common.cuh"
 #include "dfloat.cuh"
+#include "frico_gpu_debug.h"
 
 namespace frico {
 
@@ -41,12 +43,20 @@ namespace {
 constexpr int kGenThreads = 128;   // triangles of a chunk per generator CTA pass
 constexpr int kGenPoints = 8;      // points per generator CTA
 
-__device__ __forceinline__ float tf32_hi_f(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// x rounded to the nearest TF32 value (10 explicit mantissa bits; ties away from zero),
+// by integer operations on the magnitude bits
+__device__ __forceinline__ float tf32_rn(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
 
+// x as hi + lo, both TF32 values, rounded to nearest: |x - hi - lo| <= 2^-22 |x| with no
+// bias in sign. (Truncated splits leave lo with the sign of x, and the tensor cores'
+// truncation of lo to TF32 then shrinks every product by about 5e-7 at once, a
+// systematic error of the far-field sums.)
 __device__ __forceinline__ void put_pair(float* hp, float* lp, int64_t o, float a, float b) {
-    const float ah = tf32_hi_f(a), bh = tf32_hi_f(b);
+    const float ah = tf32_rn(a), bh = tf32_rn(b);
     *reinterpret_cast<float2*>(hp + o) = make_float2(ah, bh);
-    *reinterpret_cast<float2*>(lp + o) = make_float2(a - ah, b - bh);
+    *reinterpret_cast<float2*>(lp + o) = make_float2(tf32_rn(a - ah), tf32_rn(b - bh));
 }
 
 // B* operands of every chunk: chunk c holds rows 2j, 2j + 1 for the 3 ncols columns of
@@ -154,14 +164,6 @@ __global__ void __launch_bounds__(kGenThreads) k_ff_gen(int np, const double* __
     }
 }
 
-// S += C (FP32 chunk result into the FP64 sums), element-wise over cnt reals.
-__global__ void k_ff_accum(int64_t cnt, const float* __restrict__ C, double* __restrict__ S, int first) {
-    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-    if (i >= cnt) return;
-    const double v = double(C[i]);
-    S[i] = first ? v : S[i] + v;
-}
-
 // E[col][p0 + p][a] = -j w mu0 / (4 pi) e^{-jk|P|} (S1_a - P_a S2_0 + S2_{1+a}) for the batch.
 __global__ void k_ff_finish(int np, int ncols, const double* __restrict__ P, double k, double omega,
                             const double* __restrict__ S1, const double* __restrict__ S2, int64_t npts_total,
@@ -189,34 +191,51 @@ __global__ void k_ff_finish(int np, int ncols, const double* __restrict__ P, dou
 
 }  // namespace
 
-// Triangles per K chunk: K = 2 kc real values per product (a multiple of one 32-value slab).
-static const int kFieldsGemmKc = 128;
+// Triangles per launch (K = 2 kc real values per product): the chunk's G' and H' operands
+// for all points of a batch are materialised, the products add into the FP64 sums.
+static const int kFieldsGemmKc = 512;
+// k-steps (8 real values of K) per TMEM accumulator before its sum moves to double-float
+static const int kFieldsGemmGroup = 2;
+// diagnostic overrides of the two (frico_gpu_debug_fields_gemm_config; 0 = the defaults)
+static int g_kc_override = 0, g_group_override = 0;
+
+}  // namespace frico
+
+extern "C" int frico_gpu_debug_fields_gemm_config(int32_t kc, int32_t group) {
+    if (kc < 0 || kc % 16 != 0 || (group != 0 && group != 1 && group != 2 && group != 4)) return FRICO_GPU_EINVAL;
+    frico::g_kc_override = kc;
+    frico::g_group_override = group;
+    return FRICO_GPU_OK;
+}
+
+namespace frico {
 
 bool fields_gemm_available(frico_gpu_ctx* ctx) { return gemm_tc_available(ctx); }
 
 // E for ncols columns at npts device points dP[3 * npts] into the device array
 // E_dev[ncols][npts][3], from the lumped currents AJ[ncols][nt][3], AD[ncols][nt]
-// (device, FP64). kc <= 0: the default chunk.
+// (device, FP64). kc <= 0: the default chunk of triangles.
 int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* dP, const double2* AJ,
                      const double2* AD, double2* E_dev, int kc) {
-    if (kc <= 0) kc = kFieldsGemmKc;
+    if (kc <= 0) kc = g_kc_override > 0 ? g_kc_override : kFieldsGemmKc;
+    const int group = g_group_override > 0 ? g_group_override : kFieldsGemmGroup;
     if (kc % 16 != 0) return set_err(ctx, FRICO_GPU_EINVAL, "fields GEMM: chunk must be a multiple of 16 triangles");
     cudaStream_t st = ctx->stream;
     const int64_t nt = ctx->nt;
     const int KP = 2 * kc;
     const int nchunks = int((nt + kc - 1) / kc);
     const int cols = 7 * ncols;
-    // points per batch: keeps the chunk operands (A^ hi/lo of G' and H') and the FP64 sums
-    // of a batch below about 1 GB
-    const int64_t per_point = int64_t(4) * KP * 4 + int64_t(2) * cols * (4 + 8);
-    const int64_t np_max = std::max<int64_t>(128, (int64_t(1) << 30) / per_point);
+    // points per batch: the chunk operands (G' and H', hi and lo) and the FP64 sums of a
+    // batch stay below about 2 GB
+    const int64_t per_point = int64_t(4) * KP * 4 + int64_t(2) * cols * 8;
+    const int64_t np_max = std::max<int64_t>(128, (int64_t(1) << 31) / per_point);
     const int64_t npb = std::min<int64_t>(npts, np_max);
     const size_t a_elems = size_t(npb) * KP;
     const size_t b_elems = size_t(nchunks) * cols * 2 * KP;
-    const size_t c_elems = size_t(npb) * 2 * cols;
+    const size_t s_elems = size_t(npb) * 2 * cols;
     auto al = [](size_t bytes) { return (bytes + 1023) & ~size_t(1023); };
     const size_t bytes = 4 * al(sizeof(float) * a_elems) + 2 * al(sizeof(float) * b_elems) +
-                         al(sizeof(float) * c_elems) + al(sizeof(double) * c_elems) + 1024;
+                         al(sizeof(double) * s_elems) + 1024;
     int rc;
     if ((rc = ensure(ctx, ctx->ffws, bytes))) return rc;
     if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
@@ -229,8 +248,7 @@ int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* 
     float* Ghl = (float*)take(sizeof(float) * a_elems);
     float* Bh = (float*)take(sizeof(float) * b_elems);
     float* Bl = (float*)take(sizeof(float) * b_elems);
-    float* Cf = (float*)take(sizeof(float) * c_elems);
-    double* S = (double*)take(sizeof(double) * c_elems);
+    double* S = (double*)take(sizeof(double) * s_elems);
     const TriGeo* geo = (const TriGeo*)ctx->trigeo.p;
     {
         const int64_t total = int64_t(nchunks) * cols * kc;
@@ -243,22 +261,18 @@ int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* 
     for (int64_t p0 = 0; p0 < npts; p0 += npb) {
         const int np = int(std::min<int64_t>(npb, npts - p0));
         const double* Pb = dP + 3 * p0;
-        float* C1 = Cf;                                  // np x 6 ncols (real), column-major
-        float* C2 = Cf + size_t(np) * 6 * ncols;         // np x 8 ncols
-        double* S1 = S;
-        double* S2 = S + size_t(np) * 6 * ncols;
+        double* S1 = S;                                  // np x 6 ncols (real), column-major
+        double* S2 = S + size_t(np) * 6 * ncols;         // np x 8 ncols
         for (int c = 0; c < nchunks; c++) {
             k_ff_gen<<<unsigned((np + kGenPoints - 1) / kGenPoints), kGenThreads, 0, st>>>(
                 np, Pb, nt, int64_t(c) * kc, kc, geo, k, Ggh, Ggl, Ghh, Ghl);
+            count_launch(ctx);
             const float* B1h = Bh + size_t(c) * cols * 2 * KP;
             const float* B1l = Bl + size_t(c) * cols * 2 * KP;
             const size_t b2 = size_t(6) * ncols * KP;
-            if ((rc = gemm_tc_split_pair(ctx, st, np, KP, C1, np, 6 * ncols, Ggh, Ggl, B1h, B1l, C2, np,
-                                         8 * ncols, Ghh, Ghl, B1h + b2, B1l + b2)))
+            if ((rc = gemm_tc_dfacc_pair(ctx, st, np, KP, group, c > 0 ? 1 : 0, S1, np, 6 * ncols, Ggh,
+                                         Ggl, B1h, B1l, S2, np, 8 * ncols, Ghh, Ghl, B1h + b2, B1l + b2)))
                 return rc;
-            const int64_t cnt = int64_t(np) * 14 * ncols;
-            k_ff_accum<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, Cf, S, c == 0);
-            count_launch(ctx, 2);
         }
         const int64_t cnt = int64_t(np) * ncols;
         k_ff_finish<<<unsigned((cnt + 127) / 128), 128, 0, st>>>(np, ncols, Pb, k, omega, S1, S2, npts, p0, E_dev);

@@ -308,9 +308,11 @@ int eval_fields_multi(frico_gpu_ctx* ctx, int col0, int ncols, int64_t npts, con
     }
     const bool with_h = H_host != nullptr;
     const int fe = ctx->opt.fields_engine;
+    // AUTO: the GEMM form on the mixed path for many columns over many (point, triangle) pairs;
+    // a few points or columns (the sweep's 8 probe points) stay on the direct kernels
     const bool gemm = !with_h && (fe == FRICO_FIELDS_GEMM ||
-                                  (fe == FRICO_FIELDS_AUTO && ctx->opt.precision == FRICO_PREC_MIXED && ncols >= 4 &&
-                                   fields_gemm_available(ctx)));
+                                  (fe == FRICO_FIELDS_AUTO && ctx->opt.precision == FRICO_PREC_MIXED && ncols >= 8 &&
+                                   npts * nt >= (int64_t(1) << 24) && fields_gemm_available(ctx)));
     if (fe == FRICO_FIELDS_GEMM && !fields_gemm_available(ctx))
         return set_err(ctx, FRICO_GPU_EINVAL, "fields GEMM: tensor cores (tcgen05) not available on this device");
     if (gemm) {

@@ -25,6 +25,11 @@ int frico_gpu_debug_cgemm(frico_gpu_ctx* ctx, int32_t m, int32_t n, int32_t k, c
  * For checks that multiply with Z on the device without copying it out. */
 int frico_gpu_debug_z64(frico_gpu_ctx* ctx, const void** dev_ptr, int64_t* ld);
 
+/* The far-field GEMM form's triangles per launch (kc, a multiple of 16) and k-steps per
+ * tensor-core accumulator before its move to double-float sums (group: 1, 2 or 4); 0
+ * restores a default. Process-wide, for accuracy and speed studies. */
+int frico_gpu_debug_fields_gemm_config(int32_t kc, int32_t group);
+
 #ifdef __cplusplus
 }
 #endif

@@ -173,6 +173,37 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+                 "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                 "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                 "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
 // One problem of a launch. emit: the finished values of C also go, split into
 // hi/lo TF32, to the operand layout of a later update: 1 = as its A* (rows of
 // this C, K = this C's columns), 2 = as its B^ (row j = column j of this C).
@@ -449,6 +480,212 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_f16x3(
     const __grid_constant__ GemmArgs g) {
     gemm_body<BN, true>(tmAh0, tmAl0, tmBh0, tmBl0, tmAh1, tmAl1, tmBh1, tmBl1, g);
 }
+
+// ---- products whose sums must stay beyond FP32 accuracy (the far field, fields_gemm.cu).
+// The tensor cores accumulate in FP32 with a rounding of the running sum at every MMA,
+// which over the hundreds of MMAs of a long K loses several digits (about 1e-6 relative
+// measured over K = 256 reals). Here the MMA warp starts a fresh TMEM accumulator every
+// `group` k-steps (K = 8 per step; two accumulators of 128 columns in rotation), and the
+// epilogue warps add each finished group into double-float sums (hi + lo, two-sum on the
+// FP32 pipe) that live in the other half of TMEM (columns 256-383: hi, 384-511: lo), so
+// registers hold only the 8 columns in flight. A tile's sums go to an FP64 array C
+// (overwritten, or added to with accumulate = 1, for K split over launches). Two problems
+// per launch as above.
+struct DfProb {
+    double* C;        // M x N real, column-major, ld = ldc
+    int64_t ldc;
+    int M, N, tiles_m, tiles;
+};
+struct DfArgs {
+    DfProb p[2];
+    int nprob, KP, group, accumulate;
+    DeviceStatus* st;
+};
+static const int kDfAccs = 2;   // group accumulators in rotation (TMEM columns 0-255)
+
+__global__ void __launch_bounds__(kThreads, 1) k_gemm_dfacc(
+    const __grid_constant__ CUtensorMap tmAh0, const __grid_constant__ CUtensorMap tmAl0,
+    const __grid_constant__ CUtensorMap tmBh0, const __grid_constant__ CUtensorMap tmBl0,
+    const __grid_constant__ CUtensorMap tmAh1, const __grid_constant__ CUtensorMap tmAl1,
+    const __grid_constant__ CUtensorMap tmBh1, const __grid_constant__ CUtensorMap tmBl1,
+    const __grid_constant__ DfArgs g) {
+    constexpr int BN = 128, STAGES = Cfg<128>::STAGES, STAGE_BYTES = Cfg<128>::STAGE_BYTES;
+    constexpr int A_TILE = Cfg<128>::A_TILE, B_TILE = Cfg<128>::B_TILE, TMEM_COLS = 512;
+    constexpr uint32_t kHi = 2 * BN, kLo = 3 * BN;   // TMEM columns of the double-float sums
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char* ring = (unsigned char*)((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
+    uint64_t* bars = (uint64_t*)(ring + STAGES * STAGE_BYTES);
+    uint64_t* full = bars;                      // [STAGES]
+    uint64_t* empty = bars + STAGES;            // [STAGES]
+    uint64_t* tfull = bars + 2 * STAGES;        // [kDfAccs]
+    uint64_t* tempty = tfull + kDfAccs;         // [kDfAccs]
+    uint32_t* tmem_slot = (uint32_t*)(tempty + kDfAccs);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = g.p[0].tiles + (g.nprob > 1 ? g.p[1].tiles : 0);
+    const int kslabs = g.KP / BK;
+    const int grp = g.group, ngrp = 4 / grp;   // k-steps per accumulator, accumulators per slab
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < kDfAccs; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], kEpiWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem_base = *tmem_slot;
+    // tile t -> problem, M tile, N tile (N first: the CTAs on one A tile run together)
+    auto tile_of = [&](int t, int& pi, int& mt, int& nt_) {
+        pi = t >= g.p[0].tiles ? 1 : 0;
+        const DfProb& P = pi ? g.p[1] : g.p[0];
+        const int tt = t - (pi ? g.p[0].tiles : 0), tn = P.tiles / P.tiles_m;
+        mt = tt / tn;
+        nt_ = tt % tn;
+    };
+    if (warp == 0) {
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                int pi, mt, nt_;
+                tile_of(t, pi, mt, nt_);
+                const CUtensorMap* mAh = pi ? &tmAh1 : &tmAh0;
+                const CUtensorMap* mAl = pi ? &tmAl1 : &tmAl0;
+                const CUtensorMap* mBh = pi ? &tmBh1 : &tmBh0;
+                const CUtensorMap* mBl = pi ? &tmBl1 : &tmBl0;
+                for (int ks = 0; ks < kslabs; ks++, it++) {
+                    const int s = it % STAGES, round = it / STAGES;
+                    if (!(ok = mbar_wait(&empty[s], (round & 1) ^ 1, g.st))) break;
+                    unsigned char* base = ring + s * STAGE_BYTES;
+                    mbar_expect_tx(&full[s], STAGE_BYTES);
+                    tma_load_2d(base, mAh, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + A_TILE, mAl, &full[s], ks * BK, mt * BM);
+                    tma_load_2d(base + 2 * A_TILE, mBh, &full[s], ks * BK, nt_ * BN);
+                    tma_load_2d(base + 2 * A_TILE + B_TILE, mBl, &full[s], ks * BK, nt_ * BN);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(BM, BN);
+            int it = 0, v = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                for (int ks = 0; ks < kslabs && ok; ks++, it++) {
+                    const int s = it % STAGES, round = it / STAGES;
+                    if (!(ok = mbar_wait(&full[s], round & 1, g.st))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t base = smem_u32(ring + s * STAGE_BYTES);
+                    for (int gi = 0; gi < ngrp; gi++, v++) {
+                        const int acc = v % kDfAccs, around = v / kDfAccs;
+                        if (!(ok = mbar_wait(&tempty[acc], (around & 1) ^ 1, g.st))) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t tmem_d = tmem_base + uint32_t(acc * BN);
+                        for (int kk = gi * grp; kk < (gi + 1) * grp; kk++) {
+                            const uint32_t off = uint32_t(kk * 32);   // 8 TF32 values along K
+                            const uint64_t ah = smem_desc_sw128(base + off);
+                            const uint64_t al = smem_desc_sw128(base + A_TILE + off);
+                            const uint64_t bh = smem_desc_sw128(base + 2 * A_TILE + off);
+                            const uint64_t bl = smem_desc_sw128(base + 2 * A_TILE + B_TILE + off);
+                            mma_tf32(tmem_d, ah, bh, idesc, kk == gi * grp ? 0u : 1u);
+                            mma_tf32(tmem_d, ah, bl, idesc, 1u);
+                            mma_tf32(tmem_d, al, bh, idesc, 1u);
+                        }
+                        mma_commit(&tfull[acc]);
+                    }
+                    if (!ok) break;
+                    mma_commit(&empty[s]);
+                }
+            }
+        }
+    } else {
+        // epilogue warps 2..9: TMEM lane quadrant q = warp % 4, columns [h, h + 64), 8 at a time
+        const int q = warp & 3, h = ((warp - 2) >> 2) * 64;
+        const int row = q * 32 + lane;
+        const uint32_t lanes = uint32_t(q * 32) << 16;
+        int v = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            int pi, mt, nt_;
+            tile_of(t, pi, mt, nt_);
+            const DfProb P = pi ? g.p[1] : g.p[0];
+            for (int ks = 0; ks < kslabs && ok; ks++) {
+                for (int gi = 0; gi < ngrp; gi++, v++) {
+                    const int acc = v % kDfAccs, around = v / kDfAccs;
+                    if (!(ok = mbar_wait(&tfull[acc], around & 1, g.st))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const bool first = ks == 0 && gi == 0;
+#pragma unroll 1
+                    for (int c0 = 0; c0 < 64; c0 += 8) {
+                        const uint32_t col = uint32_t(h + c0);
+                        float x[8], hi[8], lo[8];
+                        tmem_ld8(tmem_base + lanes + uint32_t(acc * BN) + col, x);
+                        if (first) {
+#pragma unroll
+                            for (int j = 0; j < 8; j++) {
+                                hi[j] = x[j];
+                                lo[j] = 0.f;
+                            }
+                        } else {
+                            tmem_ld8(tmem_base + lanes + kHi + col, hi);
+                            tmem_ld8(tmem_base + lanes + kLo + col, lo);
+#pragma unroll
+                            for (int j = 0; j < 8; j++) {   // (hi, lo) += x, two-sum
+                                const float a = hi[j], b = x[j];
+                                const float sm = __fadd_rn(a, b);
+                                const float bv = __fsub_rn(sm, a);
+                                const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(sm, bv)), __fsub_rn(b, bv));
+                                hi[j] = sm;
+                                lo[j] = __fadd_rn(lo[j], e);
+                            }
+                        }
+                        tmem_st8(tmem_base + lanes + kHi + col, hi);
+                        tmem_st8(tmem_base + lanes + kLo + col, lo);
+                    }
+                    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty[acc]);
+                }
+            }
+            if (!ok) break;
+            const int gr = mt * BM + row;
+            const int ncol = min(64, P.N - nt_ * BN - h);
+            double* cp = P.C + int64_t(nt_ * BN + h) * P.ldc + gr;
+#pragma unroll 1
+            for (int c0 = 0; c0 < 64; c0 += 8) {
+                float hi[8], lo[8];
+                tmem_ld8(tmem_base + lanes + kHi + uint32_t(h + c0), hi);
+                tmem_ld8(tmem_base + lanes + kLo + uint32_t(h + c0), lo);
+                if (gr < P.M)
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        if (c0 + j < ncol) {
+                            const double r = double(hi[j]) + double(lo[j]);
+                            double* o = cp + int64_t(c0 + j) * P.ldc;
+                            *o = g.accumulate ? *o + r : r;
+                        }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS));
+    }
+}
+
+static constexpr int kDfSmemBytes = Cfg<128>::STAGES * Cfg<128>::STAGE_BYTES + 1024 + 256;
 
 // Store x as a hi/lo operand pair at element o: TF32 (float arrays) or, with a
 // scale, FP16 (__half arrays).
@@ -754,6 +991,43 @@ int gemm_tc_split_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, float
     q[1].p.ldc = ldc2;
     q[0].p.nfast = q[1].p.nfast = 1;
     return launch_gemm(ctx, st, q, 2, KP, 0, nullptr);
+}
+
+// Two independent real products C_i (+)= A_i B_i^T with sums in double-float: as
+// gemm_tc_split_pair, but C_i is FP64 (M x N_i, column-major, ld ldc_i doubles),
+// overwritten (accumulate = 0) or added to (1); a fresh TMEM accumulator every `group`
+// k-steps (1, 2 or 4).
+int gemm_tc_dfacc_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, int group, int accumulate, double* C1,
+                       int64_t ldc1, int N1, const float* A1h, const float* A1l, const float* B1h, const float* B1l,
+                       double* C2, int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
+                       const float* B2l) {
+    if (KP % tc::BK != 0 || M <= 0 || N1 <= 0 || N2 <= 0 || ldc1 < M || ldc2 < M ||
+        (group != 1 && group != 2 && group != 4))
+        return set_err(ctx, FRICO_GPU_EINVAL, "gemm_tc_dfacc_pair: bad shape");
+    int rc;
+    if ((rc = device_once(ctx, kOnceGemmDf, [](frico_gpu_ctx* c) {
+             return cuda_check(c, cudaFuncSetAttribute(tc::k_gemm_dfacc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       tc::kDfSmemBytes), "dfacc smem attribute");
+         })))
+        return rc;
+    TcProblem q[2];
+    if ((rc = make_problem(ctx, q[0], nullptr, 0, M, N1, A1h, A1l, B1h, B1l, KP, 0, 0, nullptr, nullptr))) return rc;
+    if ((rc = make_problem(ctx, q[1], nullptr, 0, M, N2, A2h, A2l, B2h, B2l, KP, 0, 0, nullptr, nullptr))) return rc;
+    tc::DfArgs a;
+    a.p[0] = tc::DfProb{C1, ldc1, M, N1, q[0].p.tiles_m, q[0].p.tiles};
+    a.p[1] = tc::DfProb{C2, ldc2, M, N2, q[1].p.tiles_m, q[1].p.tiles};
+    a.nprob = 2;
+    a.KP = KP;
+    a.group = group;
+    a.accumulate = accumulate;
+    a.st = (DeviceStatus*)ctx->status.p;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int ntiles = a.p[0].tiles + a.p[1].tiles;
+    tc::k_gemm_dfacc<<<std::min(ntiles, sms), tc::kThreads, tc::kDfSmemBytes, st>>>(
+        q[0].mah, q[0].mal, q[0].mbh, q[0].mbl, q[1].mah, q[1].mal, q[1].mbh, q[1].mbl, a);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "k_gemm_dfacc");
 }
 
 // ---- the no-pivot LU's block column in three launches (see lu_nopiv.cu)

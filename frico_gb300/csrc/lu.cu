@@ -996,6 +996,43 @@ int lu_solve_fp64(frico_gpu_ctx* ctx, double2* B, int nrhs, int64_t ldb) {
     return FRICO_GPU_OK;
 }
 
+__global__ void k_add_c128(int64_t count, const double2* __restrict__ d, double2* __restrict__ x) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < count) x[i] = cadd(x[i], d[i]);
+}
+
+// One step of FP64 iterative refinement of the FP64 drop-in's solution X (n x nrhs,
+// ld n) of Zk X = B, Zk the matrix the resident factors came from (kept before the
+// in-place factorisation): R = B - Zk X, X += (LU)^{-1} R. The chained solves apply
+// explicit inverses of their 64 x 64 diagonal blocks, which is not backward stable
+// when those blocks are ill-conditioned (the EFIE at low frequency); one step brings
+// the backward error to that of a substitution solve such as LAPACK's zgetrs.
+int refine_fp64_once(frico_gpu_ctx* ctx, const double2* Zk, const double2* B, double2* X) {
+    const int64_t n = ctx->n;
+    const int nrhs = ctx->nrhs;
+    const int64_t cnt = n * nrhs;
+    cudaStream_t st = ctx->stream;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const unsigned rblocks = unsigned((n + 255) / 256);
+    int nchunks = std::max(1, std::min(int(n / 128), int((4 * sms + rblocks - 1) / rblocks)));
+    const int chunk = int((n + nchunks - 1) / nchunks);
+    nchunks = int((n + chunk - 1) / chunk);
+    int rc;
+    if ((rc = ensure(ctx, ctx->rwork32, sizeof(double2) * size_t(nchunks) * nrhs * n))) return rc;
+    if ((rc = ensure(ctx, ctx->res64, sizeof(double2) * cnt))) return rc;
+    double2* part = (double2*)ctx->rwork32.p;
+    double2* R = (double2*)ctx->res64.p;
+    k_residual_part<<<dim3(rblocks, nchunks), 256, 0, st>>>(Zk, n, int(n), X, n, nrhs, chunk, part);
+    k_residual_reduce<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(int(n), nrhs, nchunks, part, B, n, R);
+    count_launch(ctx, 2);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "fp64 refinement residual"))) return rc;
+    if ((rc = lu_solve_fp64(ctx, R, nrhs, n))) return rc;
+    k_add_c128<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, R, X);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), "fp64 refinement update");
+}
+
 __global__ void k_matvec_reduce(int64_t cnt, int nchunks, const double2* __restrict__ part,
                                 double2* __restrict__ Y) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;

@@ -12,8 +12,6 @@
 // Per block column k0 (width nb = 128):
 //   k_diag_lu      two CTAs, one elimination sweep each: LU and L11^{-1} of the
 //                  nb x nb diagonal block, and U11^{-1} as the rows of U appear
-//                  (SIMT and 3xFP16 engines; the 3xTF32 tensor-core path uses the
-//                  blocked k_diag_lu_blk of diag_blocked.cu)
 //   k_trsm_right   L21 = A21 U11^{-1}, 64 rows per CTA
 //   k_trsm_lower_unit (lu.cu)   U12 = L11^{-1} A12
 //   trailing update A22 -= L21 U12 (tensor cores when available)
@@ -447,10 +445,6 @@ __global__ void __launch_bounds__(256) k_trsm_right(C* A, int64_t lda, int r0, i
 }
 
 // ------------------------------------------------------------------ host side
-int launch_diag_lu_blk(frico_gpu_ctx* ctx, cudaStream_t st, const float2* src, int64_t lds, float2* dlu, int64_t ldd,
-                       int k0, int jb, float2* Uinv, float2* Linv, DeviceStatus* dst, const TcDiagSplit& sp);
-int diag_lu_blk_setup(frico_gpu_ctx* ctx);   // diag_blocked.cu
-
 template <typename C> __global__ void k_ipiv_identity(int n, int32_t* ipiv, int32_t* perm) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
@@ -489,8 +483,6 @@ static int launch_diag_lu(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, int64_
         lds = kNP;
     }
     TcDiagSplit none{};
-    if (stage && !(sp && sp->h))   // tensor-core path, 3xTF32 operands: the blocked kernel (diag_blocked.cu)
-        return launch_diag_lu_blk(ctx, st, src, lds, dlu, ldd, k0, jb, Uinv, Linv, dst, sp ? *sp : none);
     if (sp && sp->h)
         k_diag_lu<float2, true><<<2, kDiagThreads, diag_lu_smem<float2>(), st>>>(src, lds, dlu, ldd, k0, jb, Uinv,
                                                                                  Linv, dst, *sp);
@@ -604,7 +596,6 @@ int lu_factor_nopiv_fp32(frico_gpu_ctx* ctx) {
              r = cuda_check(c, cudaFuncSetAttribute(k_diag_lu<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     int(diag_lu_smem<float2>())), "diag smem");
              if (r) return r;
-             if ((r = diag_lu_blk_setup(c))) return r;
              r = cuda_check(c, cudaFuncSetAttribute(k_uinv_blocks<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     int(uinv_smem<float2>())), "uinv smem");
              if (r) return r;

@@ -100,8 +100,9 @@ typedef struct frico_gpu_options {
     int32_t fields_engine;   /* FRICO_FIELDS_*: E of many right-hand sides (eval_fields_multi) */
 } frico_gpu_options;
 
-#define FRICO_FIELDS_AUTO   0  /* mixed precision: E of >= 4 columns as tensor-core GEMMs (tcgen05 3xTF32,
-                                  FP64 phase and sums); FP64 precision and H: the direct kernels */
+#define FRICO_FIELDS_AUTO   0  /* mixed precision: E of >= 8 columns over >= 2^24 (point, triangle) pairs as
+                                  tensor-core GEMMs (tcgen05 3xTF32, FP64 phase, double-float sums);
+                                  otherwise, FP64 precision and H: the direct kernels */
 #define FRICO_FIELDS_DIRECT 1  /* direct (point, triangle) kernels: FP64, or double-float for mixed */
 #define FRICO_FIELDS_GEMM   2  /* E as tensor-core GEMMs whatever the precision (error if unavailable) */
 
@@ -353,7 +354,7 @@ int frico_gpu_adjoint(frico_gpu_ctx* ctx, double freq, int32_t n_itf, const int3
  * With fields_engine selecting GEMMs (and H not asked for), E comes from two
  * complex matrix products over the triangles on the tensor cores: the Green
  * function with the point's phase e^{-jk|P|} factored out, times the lumped
- * currents (accurate to ~1e-7 of |E|, against ~1e-12 for the direct kernels). */
+ * currents (errors of a few 1e-7 of |E|, against ~1e-12 for the direct kernels). */
 int frico_gpu_eval_fields_multi(frico_gpu_ctx* ctx, int32_t col0, int32_t ncols, int64_t npts,
                                 const double* P, frico_c128* E, frico_c128* H);
 /* bistatic_RCS_unit_Ei at sph2rect(R, theta[i], phi[i]) for every column:

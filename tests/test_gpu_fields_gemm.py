@@ -50,8 +50,9 @@ def test_fields_engine_auto_picks_gemm_for_many_columns(gpu_lib):
     """Mixed precision with the default engine evaluates E of many columns as GEMMs
     (results equal the forced GEMM engine's bit for bit) and keeps the direct
     kernels for the FP64 drop-in and whenever H is asked for."""
-    sim = _solved(2, 300e6, 6, "mixed")
-    pts = meshes.sph2rect(10.0, np.linspace(0, np.pi, 50), np.zeros(50))
+    sim = _solved(3, 450e6, 8, "mixed")     # 1280 triangles x 16384 points = 2^24.3 pairs
+    rng = np.random.default_rng(3)
+    pts = meshes.sph2rect(10.0, np.arccos(rng.uniform(-1, 1, 16384)), rng.uniform(0, 2 * np.pi, 16384))
     E_auto, _ = sim.eval_fields_multi(pts, want_h=False)
     sim.set_options(fields_engine=2)
     E_gemm, _ = sim.eval_fields_multi(pts, want_h=False)
