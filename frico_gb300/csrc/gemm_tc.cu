@@ -30,7 +30,8 @@
 //   warp 0      TMA producer: per 128-byte K slab (32 TF32 or 64 FP16 values),
 //               the four 128-row operand tiles (A hi/lo, B hi/lo) into a
 //               3-stage shared-memory ring, 128-byte swizzle.
-//   warp 1      allocates 256 TMEM columns (two 128 x 128 FP32 accumulators)
+//   warp 1      allocates all 512 TMEM columns (four 128 x 128 FP32 accumulators
+//               in rotation, so the MMAs can run up to three tiles ahead of the epilogue)
 //               and issues tcgen05.mma (M = 128, N = 128, K = 8 per
 //               instruction); tcgen05.commit frees ring stages and publishes
 //               finished accumulators.
@@ -69,7 +70,8 @@ template <int BN> struct Cfg {
     static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
     static constexpr int STAGING = 8 * 32 * 32 * 4;   // per epilogue warp a 32 x 32 float block (A* emission)
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGING + 1024 + 256;
-    static constexpr int TMEM_COLS = 2 * BN;
+    static constexpr int ACCS = 512 / BN;   // TMEM accumulators in rotation (all 512 columns)
+    static constexpr int TMEM_COLS = ACCS * BN;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -264,9 +266,10 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
     uint64_t* bars = (uint64_t*)(ring + STAGES * STAGE_BYTES);
     uint64_t* full = bars;                 // [STAGES]
     uint64_t* empty = bars + STAGES;       // [STAGES]
-    uint64_t* tfull = bars + 2 * STAGES;   // [2]
-    uint64_t* tempty = bars + 2 * STAGES + 2;  // [2]
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 4);
+    constexpr int ACCS = Cfg<BN>::ACCS;
+    uint64_t* tfull = bars + 2 * STAGES;          // [ACCS]
+    uint64_t* tempty = bars + 2 * STAGES + ACCS;  // [ACCS]
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 2 * ACCS);
     float* staging = (float*)(ring + STAGES * STAGE_BYTES + 256);   // 8 x 32 x 32 floats
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -278,7 +281,7 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int a = 0; a < 2; a++) {
+        for (int a = 0; a < ACCS; a++) {
             mbar_init(&tfull[a], 1);
             mbar_init(&tempty[a], kEpiWarps);
         }
@@ -325,7 +328,7 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
             int it = 0, tcount = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, tcount++) {
-                const int acc = tcount & 1, around = tcount >> 1;
+                const int acc = tcount % ACCS, around = tcount / ACCS;
                 if (!(ok = mbar_wait(&tempty[acc], (around & 1) ^ 1, g.st))) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t tmem_d = tmem_base + uint32_t(acc * BN);
@@ -364,7 +367,7 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
         const int row = q * 32 + lane;
         int tcount = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, tcount++) {
-            const int acc = tcount & 1, around = tcount >> 1;
+            const int acc = tcount % ACCS, around = tcount / ACCS;
             const int pi = t >= g.p[0].tiles ? 1 : 0;
             const GemmProb P = pi ? g.p[1] : g.p[0];
             const int tt = t - (pi ? g.p[0].tiles : 0), tn = P.tiles / P.tiles_m;
