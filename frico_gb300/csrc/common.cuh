@@ -318,9 +318,9 @@ int gemm_tc_split_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, float
                        const float* A1h, const float* A1l, const float* B1h, const float* B1l, float* C2,
                        int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
                        const float* B2l);   // gemm_tc.cu
-int gemm_tc_dfacc_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, int group, int accumulate, double* C1,
+int gemm_tc_dfacc_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, int group, int accumulate, float2* C1,
                        int64_t ldc1, int N1, const float* A1h, const float* A1l, const float* B1h, const float* B1l,
-                       double* C2, int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
+                       float2* C2, int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
                        const float* B2l);   // gemm_tc.cu
 bool fields_gemm_available(frico_gpu_ctx* ctx);                // fields_gemm.cu
 int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* dP, const double2* AJ,

@@ -16,7 +16,7 @@
 // products run on the tcgen05 3xTF32 tensor cores (gemm_tc.cu, k_gemm_dfacc) with
 // the currents as the B operand; every k-step's TMEM result is moved into
 // double-float sums (the FP32 tensor-core accumulation spans 3 MMAs only), and the
-// triangle chunks add into FP64 sums. The point phase e^{-jk|P|} and the final
+// triangle chunks add into double-float sums. The point phase e^{-jk|P|} and the final
 // combination are FP64.
 //
 // Real-GEMM layout of the complex products (A^ real, B* doubled):
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kGenThreads) k_ff_gen(int np, const double* __
 
 // E[col][p0 + p][a] = -j w mu0 / (4 pi) e^{-jk|P|} (S1_a - P_a S2_0 + S2_{1+a}) for the batch.
 __global__ void k_ff_finish(int np, int ncols, const double* __restrict__ P, double k, double omega,
-                            const double* __restrict__ S1, const double* __restrict__ S2, int64_t npts_total,
+                            const float2* __restrict__ S1, const float2* __restrict__ S2, int64_t npts_total,
                             int64_t p0, double2* __restrict__ E) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= int64_t(np) * ncols) return;
@@ -178,8 +178,9 @@ __global__ void k_ff_finish(int np, int ncols, const double* __restrict__ P, dou
     // -j w mu0 / (4 pi) e^{-jk|P|}
     const double m = omega * FRICO_MU0 * 0.25 * M_1_PI;
     const double2 pre = make_double2(-m * s, -m * c);
-    auto at = [&](const double* S, int j) {   // complex column j, point p
-        return make_double2(S[int64_t(2 * j) * np + p], S[int64_t(2 * j + 1) * np + p]);
+    auto at = [&](const float2* S, int j) {   // complex column j, point p, from its double-float parts
+        const float2 re = S[int64_t(2 * j) * np + p], im = S[int64_t(2 * j + 1) * np + p];
+        return make_double2(double(re.x) + double(re.y), double(im.x) + double(im.y));
     };
     const double2 s20 = at(S2, 4 * col);
     for (int a = 0; a < 3; a++) {
@@ -192,7 +193,7 @@ __global__ void k_ff_finish(int np, int ncols, const double* __restrict__ P, dou
 }  // namespace
 
 // Triangles per launch (K = 2 kc real values per product): the chunk's G' and H' operands
-// for all points of a batch are materialised, the products add into the FP64 sums.
+// for all points of a batch are materialised, the products add into the double-float sums.
 static const int kFieldsGemmKc = 512;
 // k-steps (8 real values of K) per TMEM accumulator before its sum moves to double-float
 static const int kFieldsGemmGroup = 2;
@@ -235,7 +236,7 @@ int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* 
     const size_t s_elems = size_t(npb) * 2 * cols;
     auto al = [](size_t bytes) { return (bytes + 1023) & ~size_t(1023); };
     const size_t bytes = 4 * al(sizeof(float) * a_elems) + 2 * al(sizeof(float) * b_elems) +
-                         al(sizeof(double) * s_elems) + 1024;
+                         al(sizeof(float2) * s_elems) + 1024;
     int rc;
     if ((rc = ensure(ctx, ctx->ffws, bytes))) return rc;
     if ((rc = ensure(ctx, ctx->status, sizeof(DeviceStatus)))) return rc;
@@ -248,7 +249,7 @@ int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* 
     float* Ghl = (float*)take(sizeof(float) * a_elems);
     float* Bh = (float*)take(sizeof(float) * b_elems);
     float* Bl = (float*)take(sizeof(float) * b_elems);
-    double* S = (double*)take(sizeof(double) * s_elems);
+    float2* S = (float2*)take(sizeof(float2) * s_elems);   // double-float (hi, lo) sums
     const TriGeo* geo = (const TriGeo*)ctx->trigeo.p;
     {
         const int64_t total = int64_t(nchunks) * cols * kc;
@@ -261,8 +262,8 @@ int eval_fields_gemm(frico_gpu_ctx* ctx, int ncols, int64_t npts, const double* 
     for (int64_t p0 = 0; p0 < npts; p0 += npb) {
         const int np = int(std::min<int64_t>(npb, npts - p0));
         const double* Pb = dP + 3 * p0;
-        double* S1 = S;                                  // np x 6 ncols (real), column-major
-        double* S2 = S + size_t(np) * 6 * ncols;         // np x 8 ncols
+        float2* S1 = S;                                  // np x 6 ncols (real), column-major
+        float2* S2 = S + size_t(np) * 6 * ncols;         // np x 8 ncols
         for (int c = 0; c < nchunks; c++) {
             k_ff_gen<<<unsigned((np + kGenPoints - 1) / kGenPoints), kGenThreads, 0, st>>>(
                 np, Pb, nt, int64_t(c) * kc, kc, geo, k, Ggh, Ggl, Ghh, Ghl);

@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_f16x3(
 // (overwritten, or added to with accumulate = 1, for K split over launches). Two problems
 // per launch as above.
 struct DfProb {
-    double* C;        // M x N real, column-major, ld = ldc
+    float2* C;        // M x N real double-float values (hi, lo), column-major, ld = ldc
     int64_t ldc;
     int M, N, tiles_m, tiles;
 };
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_dfacc(
             if (!ok) break;
             const int gr = mt * BM + row;
             const int ncol = min(64, P.N - nt_ * BN - h);
-            double* cp = P.C + int64_t(nt_ * BN + h) * P.ldc + gr;
+            float2* cp = P.C + int64_t(nt_ * BN + h) * P.ldc + gr;
 #pragma unroll 1
             for (int c0 = 0; c0 < 64; c0 += 8) {
                 float hi[8], lo[8];
@@ -674,9 +674,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_dfacc(
 #pragma unroll
                     for (int j = 0; j < 8; j++)
                         if (c0 + j < ncol) {
-                            const double r = double(hi[j]) + double(lo[j]);
-                            double* o = cp + int64_t(c0 + j) * P.ldc;
-                            *o = g.accumulate ? *o + r : r;
+                            // double-float on the FP32 pipe (the FP64 pipe is narrow on this part)
+                            float2* o = cp + int64_t(c0 + j) * P.ldc;
+                            float h2 = hi[j], l2 = lo[j];
+                            if (g.accumulate) {
+                                const float2 c = *o;
+                                const float sm = __fadd_rn(c.x, h2);
+                                const float bv = __fsub_rn(sm, c.x);
+                                const float e = __fadd_rn(__fsub_rn(c.x, __fsub_rn(sm, bv)), __fsub_rn(h2, bv));
+                                h2 = sm;
+                                l2 = __fadd_rn(__fadd_rn(c.y, l2), e);
+                            }
+                            const float r = __fadd_rn(h2, l2);   // renormalise: |lo| <= ulp(hi) / 2
+                            *o = make_float2(r, __fsub_rn(l2, __fsub_rn(r, h2)));
                         }
             }
         }
@@ -997,12 +1007,13 @@ int gemm_tc_split_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, float
 }
 
 // Two independent real products C_i (+)= A_i B_i^T with sums in double-float: as
-// gemm_tc_split_pair, but C_i is FP64 (M x N_i, column-major, ld ldc_i doubles),
+// gemm_tc_split_pair, but C_i holds double-float (hi, lo) pairs (M x N_i, column-major,
+// ld ldc_i pairs),
 // overwritten (accumulate = 0) or added to (1); a fresh TMEM accumulator every `group`
 // k-steps (1, 2 or 4).
-int gemm_tc_dfacc_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, int group, int accumulate, double* C1,
+int gemm_tc_dfacc_pair(frico_gpu_ctx* ctx, cudaStream_t st, int M, int KP, int group, int accumulate, float2* C1,
                        int64_t ldc1, int N1, const float* A1h, const float* A1l, const float* B1h, const float* B1l,
-                       double* C2, int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
+                       float2* C2, int64_t ldc2, int N2, const float* A2h, const float* A2l, const float* B2h,
                        const float* B2l) {
     if (KP % tc::BK != 0 || M <= 0 || N1 <= 0 || N2 <= 0 || ldc1 < M || ldc2 < M ||
         (group != 1 && group != 2 && group != 4))
