@@ -138,7 +138,7 @@ struct Ctx;
 
 // CUDA graph of the complex64 no-pivot factorisation (see lu_nopiv.cu).
 struct LuGraph {
-    uintptr_t key[11] = {};
+    uintptr_t key[12] = {};
     cudaGraphExec_t exec = nullptr;
     int64_t launches = 0;
     double gemm_flops = 0.0, gemm_bytes = 0.0;

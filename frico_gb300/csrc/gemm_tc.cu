@@ -88,23 +88,32 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
 // Bounded wait for the phase with the given parity; false on timeout / abort.
+// The status word (global memory, hundreds of cycles away) is polled only every
+// 256 failed tries, so that a wait that is about to end is not held up by it.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, DeviceStatus* st) {
     const uint32_t a = smem_u32(bar);
-    long long t0 = clock64();
-    while (true) {
-        uint32_t done;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if (clock64() - t0 > kWait) {
-            atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT);
-            return false;
+    if (mbar_try(a, parity)) return true;
+    const long long t0 = clock64();
+    for (uint32_t it = 1;; it++) {
+        if (mbar_try(a, parity)) return true;
+        if ((it & 15) == 0) {
+            if (clock64() - t0 > kWait) {
+                atomicCAS(&st->err, 0, FRICO_DEV_ERR_TIMEOUT);
+                return false;
+            }
+            if ((it & 255) == 0 && *(volatile int*)&st->err) return false;
         }
-        if (*(volatile int*)&st->err) return false;
     }
 }
 

@@ -511,11 +511,12 @@ static int launch_uinv_blocks(frico_gpu_ctx* ctx, cudaStream_t st, float2* A, in
 template <typename F> static int run_lu_graph(frico_gpu_ctx* ctx, F&& enqueue) {
     LuGraph& g = ctx->lu_graph;
     if (ctx->opt.profile_kernels) return enqueue();
-    const uintptr_t key[11] = {uintptr_t(ctx->n), uintptr_t(ctx->z32.p), uintptr_t(ctx->dinv128.p),
+    const uintptr_t key[12] = {uintptr_t(ctx->n), uintptr_t(ctx->z32.p), uintptr_t(ctx->dinv128.p),
                                uintptr_t(ctx->panel_ws.p), uintptr_t(ctx->tc_ws.p), uintptr_t(ctx->status.p),
                                uintptr_t(ctx->ipiv.p), uintptr_t(ctx->perm.p), uintptr_t(ctx->stream2),
-                               uintptr_t(ctx->tc_ws.bytes), uintptr_t(ctx->opt.gemm_engine)};
-    const bool same = std::equal(key, key + 11, g.key);
+                               uintptr_t(ctx->tc_ws.bytes), uintptr_t(ctx->opt.gemm_engine),
+                               uintptr_t(wait_limit(ctx))};
+    const bool same = std::equal(key, key + 12, g.key);
     cudaStream_t st = ctx->stream;
     if (same && g.exec) {
         ctx->stats.kernel_launches += g.launches;
@@ -527,7 +528,7 @@ template <typename F> static int run_lu_graph(frico_gpu_ctx* ctx, F&& enqueue) {
     if (!same) {   // first call with this key: run eagerly
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
-        std::copy(key, key + 11, g.key);
+        std::copy(key, key + 12, g.key);
         return enqueue();
     }
     const int64_t l0 = ctx->stats.kernel_launches;
