@@ -59,6 +59,7 @@ static const int BM = 128, BK = 32;              // tile rows, floats per K slab
 static const int kEpiWarps = 8;                  // epilogue warps (2 per TMEM lane quadrant)
 static const int kThreads = 64 + 32 * kEpiWarps; // producer + MMA + epilogue warps
 static const long long kWait = 4000000000LL;
+static const bool kPrefetchC = true;             // L2 prefetch of the next tile's C in the epilogue
 
 // Tile configuration by tile width BN. A stage holds A hi, A lo (128 x 32 floats
 // each) and B hi, B lo (BN x 32 floats each); the two TMEM accumulators take
@@ -392,6 +393,26 @@ __device__ __forceinline__ void gemm_body(const CUtensorMap& tmAh0, const CUtens
                 esc = pow_scale(P.esp, P.ec, P.ep);
             }
             float* cp = P.C + int64_t(nt_ * BN + h) * ldc + gr;
+            // the C lines of this warp's part of the CTA's next tile into L2 (each lane two of the
+            // 64 128-byte column segments), so that its loads there wait on L2 instead of DRAM
+            if (kPrefetchC) {
+                const int tq = t + int(gridDim.x);
+                if (tq < ntiles) {
+                    const int pq = tq >= g.p[0].tiles ? 1 : 0;
+                    const GemmProb& Q = pq ? g.p[1] : g.p[0];
+                    const int uq = tq - (pq ? g.p[0].tiles : 0), tnq = Q.tiles / Q.tiles_m;
+                    const int mq = Q.nfast ? uq / tnq : uq % Q.tiles_m, nq = Q.nfast ? uq % tnq : uq / Q.tiles_m;
+                    const int r0 = mq * BM + q * 32;
+                    if (Q.accumulate && r0 < Q.M) {
+#pragma unroll
+                        for (int k = 0; k < 2; k++) {
+                            const int j = lane + 32 * k;
+                            if (nq * BN + h + j < Q.N)
+                                asm volatile("prefetch.global.L2 [%0];" ::"l"(Q.C + int64_t(nq * BN + h + j) * Q.ldc + r0));
+                        }
+                    }
+                }
+            }
             // C values first: these reads do not depend on the accumulator
             float cv[64];
             if (accumulate && rowok && ncol == 64) {
