@@ -14,9 +14,9 @@
 // sine / cosine in double-float, so the phase of a 190-radian path is exact to
 // ~1e-12; the values rounded to FP32), written split into TF32 hi / lo; the
 // products run on the tcgen05 3xTF32 tensor cores (gemm_tc.cu, k_gemm_dfacc) with
-// the currents as the B operand; every k-step's TMEM result is moved into
-// double-float sums (the FP32 tensor-core accumulation spans 3 MMAs only), and the
-// triangle chunks add into double-float sums. The point phase e^{-jk|P|} and the final
+// the currents as the B operand; the TMEM result of every second k-step is moved
+// into double-float sums (the FP32 tensor-core accumulation spans 6 MMAs only), and
+// the triangle chunks add into double-float sums. The point phase e^{-jk|P|} and the final
 // combination are FP64.
 //
 // Real-GEMM layout of the complex products (A^ real, B* doubled):
