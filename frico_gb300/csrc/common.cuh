@@ -37,6 +37,21 @@ template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
     return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
 }
 template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) { return {a.x * s, a.y * s}; }
+// acc += a*b as four fused multiply-adds (written as acc += x*y - z*w the compiler forms
+// the difference first: a multiply, an FMA and an add per part)
+template <typename C> __device__ __forceinline__ void cmac(C& acc, C a, C b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a)*b, four fused multiply-adds
+template <typename C> __device__ __forceinline__ void cmac_conj(C& acc, C a, C b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+}
 // a - b*c
 template <typename C> __host__ __device__ __forceinline__ C cfms(C a, C b, C c) {
     return {a.x - b.x * c.x + b.y * c.y, a.y - b.x * c.y - b.y * c.x};

@@ -45,8 +45,7 @@ __global__ void __launch_bounds__(256) k_gs_dots(int n, const double2* __restric
     double2 acc = make_double2(0, 0);
     for (int r = threadIdx.x; r < n; r += 256) {
         const double2 a = v[r], b = w[r];
-        acc.x += a.x * b.x + a.y * b.y;
-        acc.y += a.x * b.y - a.y * b.x;
+        cmac_conj(acc, a, b);
     }
     for (int o = 16; o > 0; o >>= 1) {
         acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);

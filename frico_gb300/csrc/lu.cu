@@ -429,8 +429,7 @@ __global__ void __launch_bounds__(256) k_gemm_update(cplx<R>* Cm, int64_t ldc, c
             for (int i = 0; i < 4; i++)
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    acc[i][j].x += a[i].x * b[j].x - a[i].y * b[j].y;
-                    acc[i][j].y += a[i].x * b[j].y + a[i].y * b[j].x;
+                    cmac(acc[i][j], a[i], b[j]);
                 }
         }
         __syncthreads();
@@ -506,8 +505,7 @@ __global__ void __launch_bounds__(256) k_residual_part(const double2* __restrict
                     for (int ii = 0; ii < ni; ii++) {
                         double2 z = zp[int64_t(ii) * ldz];
                         double2 x = xs[ii];
-                        acc[0].x += z.x * x.x - z.y * x.y;
-                        acc[0].y += z.x * x.y + z.y * x.x;
+                        cmac(acc[0], z, x);
                     }
                 } else {
                     for (int ii = 0; ii < ni; ii++) {
@@ -516,8 +514,7 @@ __global__ void __launch_bounds__(256) k_residual_part(const double2* __restrict
                         for (int c = 0; c < kTR; c++)
                             if (c < nc) {
                                 double2 x = xs[c * 128 + ii];
-                                acc[c].x += z.x * x.x - z.y * x.y;
-                                acc[c].y += z.x * x.y + z.y * x.x;
+                                cmac(acc[c], z, x);
                             }
                     }
                 }

@@ -433,8 +433,7 @@ __global__ void __launch_bounds__(256) k_trsm_right(C* A, int64_t lda, int r0, i
 #pragma unroll
             for (int j = 0; j < 32; j++) {
                 const C w = u[(c0 + j) * jb + q];   // broadcast
-                acc[j].x += x.x * w.x - x.y * w.y;
-                acc[j].y += x.x * w.y + x.y * w.x;
+                cmac(acc[j], x, w);
             }
         }
         if (row < nr)
