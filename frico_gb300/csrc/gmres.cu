@@ -22,6 +22,7 @@
 namespace frico {
 
 int matvec_fp64(frico_gpu_ctx* ctx, const double2* X, int nrhs, double2* Y);                          // lu.cu
+int matvec_z64(frico_gpu_ctx* ctx, const double2* X, int nrhs, double2* Y, bool df);                 // lu.cu
 int precond_apply_fp32(frico_gpu_ctx* ctx, const double2* In, int64_t ld_in, int nrhs, double2* Out);  // lu.cu
 
 namespace {
@@ -124,6 +125,11 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
     const int64_t ldz = int64_t(m) * n;       // preconditioned basis: Zb + c ldz, vector i at + i n
     cudaStream_t st = ctx->stream;
     int rc;
+    // Arnoldi products in double-float (the restarts' true residuals stay FP64)
+    bool use_df = ctx->opt.residual_mode == FRICO_RESIDUAL_AUTO;
+    if (use_df && (rc = cuda_check(ctx, cudaMemsetAsync(&((DeviceStatus*)ctx->status.p)->df_range, 0, sizeof(int),
+                                                        st), "df flag")))
+        return rc;
     const size_t vbytes = sizeof(double2) * size_t(nrhs) * (ldc + ldz);
     const size_t wbytes = sizeof(double2) * size_t(cnt);
     const size_t hbytes = sizeof(double2) * size_t(nrhs) * (m + 1);
@@ -186,23 +192,32 @@ int gmres_refine(frico_gpu_ctx* ctx, double2* X, const double2* B, double2* R, c
                                                         sizeof(double2) * n, sizeof(double2) * n, nrhs,
                                                         cudaMemcpyDeviceToDevice, st), "gmres z")))
                 return rc;
-            if ((rc = matvec_fp64(ctx, U, nrhs, W))) return rc;
-            for (int pass = 0; pass < 2; pass++) {
-                double2* hp = dh + size_t(pass) * nrhs * (m + 1);
-                k_gs_dots<<<dim3(j + 1, nrhs), 256, 0, st>>>(n, V, ldc, W, hp, m + 1);
-                k_gs_axpy<<<g1, 256, 0, st>>>(n, nrhs, j + 1, V, ldc, hp, m + 1, W);
-                count_launch(ctx, 2);
+            // W = Z U, orthogonalised against V (two classical Gram-Schmidt passes), its norms
+            auto arnoldi = [&](bool df) -> int {
+                int r2 = matvec_z64(ctx, U, nrhs, W, df);
+                if (r2) return r2;
+                for (int pass = 0; pass < 2; pass++) {
+                    double2* hp = dh + size_t(pass) * nrhs * (m + 1);
+                    k_gs_dots<<<dim3(j + 1, nrhs), 256, 0, st>>>(n, V, ldc, W, hp, m + 1);
+                    k_gs_axpy<<<g1, 256, 0, st>>>(n, nrhs, j + 1, V, ldc, hp, m + 1, W);
+                    count_launch(ctx, 2);
+                }
+                k_norm2_cols<<<nrhs, 256, 0, st>>>(n, W, dnr);
+                count_launch(ctx);
+                r2 = cuda_check(ctx, cudaMemcpyAsync(hh.data(), dh, sizeof(double2) * hh.size(), cudaMemcpyDeviceToHost,
+                                                     st), "gmres h");
+                if (!r2)
+                    r2 = cuda_check(ctx, cudaMemcpyAsync(hnorm.data(), dnr, sizeof(double) * nrhs,
+                                                         cudaMemcpyDeviceToHost, st), "gmres hn");
+                return r2;
+            };
+            if ((rc = arnoldi(use_df))) return rc;
+            DeviceStatus hs;
+            if ((rc = trsv_check(ctx, &hs))) return rc;   // (waits for the stream)
+            if (use_df && hs.df_range) {   // an operand outside the double-float range: FP64 from here on
+                use_df = false;
+                if ((rc = arnoldi(false)) || (rc = trsv_check(ctx))) return rc;
             }
-            k_norm2_cols<<<nrhs, 256, 0, st>>>(n, W, dnr);
-            count_launch(ctx);
-            if ((rc = cuda_check(ctx, cudaMemcpyAsync(hh.data(), dh, sizeof(double2) * hh.size(), cudaMemcpyDeviceToHost,
-                                                      st), "gmres h")))
-                return rc;
-            if ((rc = cuda_check(ctx, cudaMemcpyAsync(hnorm.data(), dnr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost,
-                                                      st), "gmres hn")))
-                return rc;
-            if ((rc = cuda_check(ctx, cudaStreamSynchronize(st), "gmres sync"))) return rc;
-            if ((rc = trsv_check(ctx))) return rc;
             bool all_done = true;
             for (int c = 0; c < nrhs; c++) {
                 hscale[c] = 0.0;

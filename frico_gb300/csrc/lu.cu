@@ -476,6 +476,13 @@ __global__ void k_gather_rows(int n, int nrhs, const int32_t* perm, const CI* B,
 
 static const int kTR = 8;    // RHS columns per residual pass
 
+// Column chunks of the residual / matvec kernels: about 4 CTAs per SM in all, chunks of
+// at least 32 columns (smaller systems get more chunks rather than idle SMs: the FP64
+// pipe, not the bandwidth, bounds these products on this part).
+static int residual_chunks(int n, int sms, int rblocks) {
+    return std::max(1, std::min(n / 32, (4 * sms + rblocks - 1) / rblocks));
+}
+
 // Partial products of the FP64 refinement residual. The FP64 pipe is narrow on
 // this part, so the work is spread over rows (256 per CTA) and over column
 // chunks (blockIdx.y): part[(y * nrhs + c) * n + r] = sum_{i in chunk y} Z[r, i] X[i, c].
@@ -1012,7 +1019,7 @@ int refine_fp64_once(frico_gpu_ctx* ctx, const double2* Zk, const double2* B, do
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const unsigned rblocks = unsigned((n + 255) / 256);
-    int nchunks = std::max(1, std::min(int(n / 128), int((4 * sms + rblocks - 1) / rblocks)));
+    int nchunks = residual_chunks(int(n), sms, int(rblocks));
     const int chunk = int((n + nchunks - 1) / nchunks);
     nchunks = int((n + chunk - 1) / chunk);
     int rc;
@@ -1040,24 +1047,43 @@ __global__ void k_matvec_reduce(int64_t cnt, int nchunks, const double2* __restr
 }
 
 // Y (n x nrhs, ld n) = Z64 X (X: n x nrhs, ld n), with the residual kernel's
-// row x column-chunk split. Workspace: ctx->rwork32.
-int matvec_fp64(frico_gpu_ctx* ctx, const double2* X, int nrhs, double2* Y) {
+// row x column-chunk split; df: the products in double-float on the FP32 pipe
+// (k_residual_part_df, about 1e-13 relative; an operand outside its exponent
+// range sets the status word's df_range, and the caller repeats the product with
+// df = false). Workspace: ctx->rwork32.
+int matvec_z64(frico_gpu_ctx* ctx, const double2* X, int nrhs, double2* Y, bool df) {
     const int64_t n = ctx->n;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const unsigned rblocks = unsigned((n + 255) / 256);
-    int nchunks = std::max(1, std::min(int(n / 128), int((4 * sms + rblocks - 1) / rblocks)));
+    int nchunks = residual_chunks(int(n), sms, int(rblocks));
     const int chunk = int((n + nchunks - 1) / nchunks);
     nchunks = int((n + chunk - 1) / chunk);
     int rc;
     if ((rc = ensure(ctx, ctx->rwork32, sizeof(double2) * size_t(nchunks) * nrhs * n))) return rc;
     double2* part = (double2*)ctx->rwork32.p;
-    k_residual_part<<<dim3(rblocks, nchunks), 256, 0, ctx->stream>>>((const double2*)ctx->z64.p, n, int(n), X, n,
-                                                                     nrhs, chunk, part);
+    const double2* Z64 = (const double2*)ctx->z64.p;
+    DeviceStatus* dst = (DeviceStatus*)ctx->status.p;
+    const dim3 grid(rblocks, nchunks);
+    cudaStream_t st = ctx->stream;
+    if (df && nrhs == 1)
+        k_residual_part_df<1><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+    else if (df && nrhs == 2)
+        k_residual_part_df<2><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+    else if (df && nrhs <= 4)
+        k_residual_part_df<4><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+    else if (df)
+        k_residual_part_df<kTR><<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part, dst);
+    else
+        k_residual_part<<<grid, 256, 0, st>>>(Z64, n, int(n), X, n, nrhs, chunk, part);
     const int64_t cnt = n * nrhs;
-    k_matvec_reduce<<<unsigned((cnt + 255) / 256), 256, 0, ctx->stream>>>(cnt, nchunks, part, Y);
+    k_matvec_reduce<<<unsigned((cnt + 255) / 256), 256, 0, st>>>(cnt, nchunks, part, Y);
     count_launch(ctx, 2);
     return cuda_check(ctx, cudaGetLastError(), "matvec");
+}
+
+int matvec_fp64(frico_gpu_ctx* ctx, const double2* X, int nrhs, double2* Y) {
+    return matvec_z64(ctx, X, nrhs, Y, false);
 }
 
 // Out (n x nrhs, ld n) = M^{-1} In for the complex64 factors (z32, perm): rows
@@ -1107,7 +1133,7 @@ int refine_solve(frico_gpu_ctx* ctx) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const unsigned rblocks = unsigned((n + 255) / 256);
-    int nchunks = std::max(1, std::min(int(n / 128), int((4 * sms + rblocks - 1) / rblocks)));
+    int nchunks = residual_chunks(int(n), sms, int(rblocks));
     const int chunk = int((n + nchunks - 1) / nchunks);
     nchunks = int((n + chunk - 1) / chunk);
     if ((rc = ensure(ctx, ctx->rwork32, sizeof(double2) * size_t(nchunks) * nrhs * n))) return rc;
