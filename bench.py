@@ -183,6 +183,73 @@ def cpu_sample(mesh, steps: int, warmup: int, Zfull=None):
     return times, os.cpu_count(), sample
 
 
+def cpu_sample_sweep(mesh, freqs, pws, feed_tags, pts):
+    """FRICO's CPU path for the bowtie sweep on a bounded sample of frequencies: per
+    frequency the fill of n/16 columns (scaled), zgetrf + zgetrs with the 4 right-hand
+    sides, port values, and per right-hand side the lumping and the 8-point field."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+    o = Oracle(mesh)
+    tags = list(feed_tags)
+    signs = o.reorient(tags)
+    n = o.n
+    cols = max(64, n // 16)
+    Z = o.compute_matrix(freqs[0])   # zgetrf's time does not depend on the frequency
+    times = []
+    for k, f in enumerate(freqs):
+        c0 = (k * cols) % max(1, n - cols)
+        t0 = time.perf_counter()
+        o.compute_matrix_cols(f, c0, c0 + cols)
+        t_fill = (time.perf_counter() - t0) * (n / cols)
+        t1 = time.perf_counter()
+        V = np.stack([o.rhs_delta_gap(f, tags, 1.0, signs)] +
+                     [o.rhs_plane_wave(f, pw.theta, pw.phi, pw.Etheta, pw.Ephi) for pw in pws], axis=1)
+        I = o.solve(Z, V)
+        o.port_values(I[:, 0], o.rwg(), tags, 1.0, signs)
+        for c in range(I.shape[1]):
+            o.lump(f, I[:, c])
+            o.eval_fields(pts)
+        times.append(t_fill + time.perf_counter() - t1)
+    sample = (f"{len(freqs)} frequencies of the band: fill of {cols}/{n} columns (scaled x{n / cols:.1f}), "
+              f"zgetrf+zgetrs with 4 RHS, port values, lumping and 8-point fields per RHS")
+    return times, os.cpu_count(), sample
+
+
+def cpu_sample_sphere64(mesh, f0, pws, T, P):
+    """FRICO's CPU path for the 64-incidence L5 step on a bounded sample: fill of n/64
+    columns (scaled), zgetrf + zgetrs of an n/4 system with the 64 right-hand sides
+    (scaled by (n / (n/4))^3 = 64), and lumping + fields of 8 of the 64 currents at
+    1024 of the points (scaled by 8 and by the point count)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+    from frico_gb300 import meshes
+    o = Oracle(mesh)
+    n = o.n
+    cols = max(64, n // 64)
+    t0 = time.perf_counter()
+    o.compute_matrix_cols(f0, 0, cols)
+    t_fill = (time.perf_counter() - t0) * (n / cols)
+    m = n // 4
+    rng = np.random.default_rng(7)
+    A = (rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))) + 4.0 * np.sqrt(m) * np.eye(m)
+    B = rng.standard_normal((m, len(pws))) + 0j
+    t1 = time.perf_counter()
+    o.solve(A, B)
+    t_lu = (time.perf_counter() - t1) * (n / m) ** 3
+    cur = o.rhs_plane_wave(f0, pws[0].theta, pws[0].phi, pws[0].Etheta, pws[0].Ephi)   # any current vector
+    idx = np.random.default_rng(5).choice(T.size, 1024, replace=False)
+    pts = meshes.sph2rect(R_FAR, T[idx], P[idx])
+    t2 = time.perf_counter()
+    for _ in range(8):
+        o.lump(f0, cur)
+        o.eval_fields(pts)
+    t_fields = (time.perf_counter() - t2) * (len(pws) / 8) * (T.size / 1024)
+    sample = (f"fill of {cols}/{n} columns (scaled x{n / cols:.0f}); zgetrf+zgetrs of a {m} x {m} system with "
+              f"{len(pws)} RHS (scaled x{(n / m) ** 3:.0f}); lumping + fields of 8 currents at 1024 of the "
+              f"{T.size} points (scaled x{len(pws) / 8 * T.size / 1024:.0f})")
+    return t_fill + t_lu + t_fields, os.cpu_count(), sample
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -506,6 +573,11 @@ def run_sweep(args):
                     "h2d_bytes_per_step": int(freqs.nbytes + pts.nbytes + 6 * 8 * 3),
                     "d2h_bytes_per_step": int(nf * (4 * 8 * 3 * 16 + 88))},
             "clocks": clk}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cf = list(all_freqs[:: max(1, len(all_freqs) // 4)])[:4]
+        ctimes, cores, csample = cpu_sample_sweep(mesh, cf, pws, feed.interfaces, pts)
+        line["cpu_baseline"] = {"value": len(ctimes) / sum(ctimes), "unit": "solves/s", "cores": cores,
+                                "kind": "port", "sample": csample}
     if rank == 0:
         print(json.dumps(line), flush=True)
     sim.close()
@@ -736,6 +808,10 @@ def run_sphere64(args):
             "sigma_rel_max": float(max(np.abs(sig_s[c] - sig_d[c]).max() / np.abs(sig_d[c]).max()
                                        for c in range(nrhs))),
             "points": 2000, "engine": "tensor-core GEMM (auto)", "bound": 1e-6}
+    if not args.no_cpu_baseline:
+        csec, cores, csample = cpu_sample_sphere64(mesh, f0, pws, T, Pg)
+        line["cpu_baseline"] = {"value": 1.0 / csec, "unit": "solves/s", "cores": cores, "kind": "port",
+                                "sample": csample}
     print(json.dumps(line), flush=True)
     sim.close()
 
