@@ -228,13 +228,16 @@ __global__ void __launch_bounds__(256) k_adj_pairs(int nt, int t_per_cta, AdjTab
                     const TermGrad g = term_grad(cmul(ui, wj[sb]), phi, R, tb.k);
                     gk = cadd(gk, g.gk);
                     for (int d = 0; d < 3; d++) {
-                        // p: A d/4 + B vr; v_ia: -A d/4; q: A e/4 - B vr; v_jb: -A e/4
-                        const double2 ad = cscale(g.A, 0.25 * d_[d]), ae = cscale(g.A, 0.25 * e[d]);
-                        const double2 bv = cscale(g.B, vr[d]);
-                        gp_c[d] = cadd(gp_c[d], cadd(ad, bv));
-                        gp_v[sa][d] = csub(gp_v[sa][d], ad);
-                        gq_c[d] = csub(gq_c[d], csub(bv, ae));
-                        gq_v[sb][d] = csub(gq_v[sb][d], ae);
+                        // p: A d/4 + B vr; v_ia: -A d/4; q: A e/4 - B vr; v_jb: -A e/4 (as FMAs)
+                        const double sd = 0.25 * d_[d], se = 0.25 * e[d], vd = vr[d];
+                        gp_c[d].x = fma(g.A.x, sd, fma(g.B.x, vd, gp_c[d].x));
+                        gp_c[d].y = fma(g.A.y, sd, fma(g.B.y, vd, gp_c[d].y));
+                        gp_v[sa][d].x = fma(-g.A.x, sd, gp_v[sa][d].x);
+                        gp_v[sa][d].y = fma(-g.A.y, sd, gp_v[sa][d].y);
+                        gq_c[d].x = fma(g.A.x, se, fma(-g.B.x, vd, gq_c[d].x));
+                        gq_c[d].y = fma(g.A.y, se, fma(-g.B.y, vd, gq_c[d].y));
+                        gq_v[sb][d].x = fma(-g.A.x, se, gq_v[sb][d].x);
+                        gq_v[sb][d].y = fma(-g.A.y, se, gq_v[sb][d].y);
                     }
                 }
             }

@@ -493,24 +493,34 @@ def test_mixed_falls_back_to_fp64_lu_when_refinement_cannot(gpu_lib, strip):
     np.testing.assert_array_equal(I2, Ir)
 
 
-def test_mixed_ill_conditioned_refines_with_gmres(gpu_lib):
+@pytest.mark.parametrize("residual", ["auto", "fp64"])
+def test_mixed_ill_conditioned_refines_with_gmres(gpu_lib, residual):
     """The 1500-unknown bowtie at 250 MHz (electrically small, with skinny
     triangles at the feed) leaves kappa * eps32 close to 1 for complex64
     factors: classical refinement contracts too slowly, and the GMRES
     refinement preconditioned by the same factors reaches the FP64 solution
-    without an FP64 factorisation."""
+    without an FP64 factorisation. residual = auto: the Arnoldi products in
+    double-float, fp64: in FP64; either way the returned currents' FP64
+    residual (recomputed on the host) is within the bound."""
     m = meshes.bowtie_preset(1500)
     f = 250e6
     dg = DeltaGap((meshes.FEED_TAG,), 1.0)
     ref = Simulation(m, precision="fp64")
     ref.run_context(f, dg)
     Ir = ref.solve()
-    mx = Simulation(m, precision="mixed")
-    mx.run_context(f, dg)
+    mx = Simulation(m, precision="mixed", residual=residual)
+    mx.delta_gap_signs = ref.delta_gap_signs
+    Z = mx.compute_matrix(f, download=True)
+    mx.set_nrhs(1)
+    mx.update_rhs(f, dg, 0)
+    B = mx.get_rhs()
     I = mx.solve()
     st = mx.stats()
     assert st["precision_used"] == 1, st
+    assert st["refine_iters"] > 6, st   # GMRES, not classical refinement alone
     assert st["refine_residual"] <= 1e-12
+    true = np.linalg.norm(B[:, 0] - Z @ I[:, 0]) / np.linalg.norm(B[:, 0])
+    assert true <= 1e-12, true
     assert rel_norm(I, Ir) < 1e-8
 
 
