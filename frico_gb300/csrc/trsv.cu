@@ -298,7 +298,14 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float2 z = make_float2(0.f, 0.f);
 
-    // independent of the chain: Dinv of this block, own right-hand side, first T block
+    // independent of the chain: Dinv of this block, own right-hand side, first T block;
+    // M_b (the last dependency's block, loaded once the one before it is in) into L2 now,
+    // so that its load on the chain waits on L2 rather than DRAM
+    if (t > 0) {
+        const char* mb = reinterpret_cast<const char*>(M + int64_t(b) * kB2 * kB2);
+        for (int line = threadIdx.x; line < kB2 * kB2 * int(sizeof(float2)) / 128; line += 512)
+            asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(mb + int64_t(line) * 128));
+    }
     const float2* D = Dinv + int64_t(b) * kB2 * kB2;
     for (int idx = threadIdx.x; idx < kB2 * kB2; idx += 512) Ds[idx] = D[idx];
     if (q == 0)
