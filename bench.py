@@ -268,7 +268,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (vector and tensor), nominal; no measured figure exists
+FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (vector and tensor), nominal; a DFMA loop on one GB300 measured 1.255
 
 
 def stage_rooflines(stage, steps, n, nt, npts, iters, green_evals, precision, hbm, bf16, f16=False):
