@@ -13,6 +13,12 @@ Fixtures (all from FRICO's code, through oracle/ref/ref_driver.cpp):
                   bistatic 359-angle sigma table
   bowtie.npz      6 x 4 bowtie: RWG table, forced delta-gap orientation signs,
                   delta-gap V with those signs
+  sphere4.npz     level-4 icosphere (N = 7680, the benchmarked size) at 450 MHz:
+                  6 seeded columns of Z, the 2-norm of every column and the
+                  Frobenius norm of Z, the plane-wave V and FRICO's solution I
+                  (solve_general); with the oracle's term magnitudes of the sampled
+                  columns (the tolerance scale where an entry's blocks cancel)
+                  (`python tests/golden/make_golden.py sphere4`: about a minute)
 """
 from __future__ import annotations
 
@@ -30,6 +36,21 @@ from frico_gb300 import meshes  # noqa: E402
 import ref_frico  # noqa: E402
 
 TRI = (np.array([0.1, 0.2, 0.3]), np.array([1.3, -0.2, 0.1]), np.array([0.4, 0.9, -0.5]))
+
+
+def make_sphere4():
+    from oracle import Oracle
+    f = 450e6
+    m = meshes.icosphere(4)
+    r = ref_frico.RefFrico(m)
+    Z = r.compute_matrix(f)
+    cols = np.sort(np.random.default_rng(20261204).choice(r.n, 6, replace=False))
+    V = r.rhs_plane_wave(f, 0.0, 0.0, 1.0, 0.0)
+    I, _, _, _ = r.run_context_plane_wave(f, 0.0, 0.0, 1.0, 0.0)
+    M = np.stack([Oracle(m).compute_matrix_magnitudes(f, int(c), int(c) + 1)[:, 0] for c in cols], axis=1)
+    np.savez_compressed(HERE / "sphere4.npz", freq=f, cols=cols, Zcols=np.ascontiguousarray(Z[:, cols]),
+                        Mcols=M, colnorms=np.linalg.norm(Z, axis=0), fro=np.linalg.norm(Z), V=V, I=I)
+    print("sphere4.npz", (HERE / "sphere4.npz").stat().st_size)
 
 
 def main():
@@ -76,4 +97,9 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["sphere4"]:
+        if not ref_frico.available():
+            raise SystemExit("oracle/_ref/libfrico_ref.so missing: build it with oracle/ref/Makefile first")
+        make_sphere4()
+    else:
+        main()

@@ -1,6 +1,10 @@
 """Pins: the oracle and the GPU library against golden vectors produced by
 FRICO's own sources (tests/golden/make_golden.py), plus a direct comparison
-with the in-place reference build where it exists."""
+with the in-place reference build where it exists.
+
+The oracle's tolerances allow a few ulps: on x86-64 the oracle reproduces the
+fixtures bit for bit, on aarch64 the C++ compiler fuses multiply-adds and the
+last bits differ (1e-15 .. 2e-14 relative measured)."""
 from pathlib import Path
 
 import numpy as np
@@ -35,10 +39,10 @@ def test_oracle_strip_golden():
     from oracle import Oracle
     g = load("strip")
     o = Oracle(meshes.strip_dipole())
-    assert np.array_equal(o.rwg(), g["rwg"])
+    assert np.allclose(o.rwg(), g["rwg"], rtol=1e-14, atol=0.0)
     f = float(g["freq"])
-    assert rel(o.compute_matrix(f), g["Z"]) < 1e-14
-    assert rel(o.compute_matrix(f, approx=True), g["Z_approx"]) < 1e-14
+    assert rel(o.compute_matrix(f), g["Z"]) < 1e-13
+    assert rel(o.compute_matrix(f, approx=True), g["Z_approx"]) < 1e-13
     V = o.rhs_delta_gap(f, FEED)
     assert rel(V, g["V"]) < 1e-15
     I = o.solve(o.compute_matrix(f), V)
@@ -70,11 +74,31 @@ def test_oracle_bowtie_golden():
     from oracle import Oracle
     g = load("bowtie")
     o = Oracle(meshes.bowtie(6, 4))
-    assert np.array_equal(o.rwg(), g["rwg"])
+    assert np.allclose(o.rwg(), g["rwg"], rtol=1e-14, atol=0.0)
     s = o.reorient(FEED, force=True)
     feed = g["signs"] != 0
     assert np.array_equal(s[feed], g["signs"][feed])
     assert rel(o.rhs_delta_gap(float(g["freq"]), FEED, 1.0, s), g["V"]) < 1e-15
+
+
+def test_oracle_sphere4_golden():
+    """The benchmarked size (level-4 sphere, N = 7680): the oracle's sampled Z columns
+    and plane-wave V against FRICO's own fill, its whole-Z column norms and Frobenius
+    norm, and its LAPACK solve against FRICO's solve_general."""
+    from oracle import Oracle
+    g = load("sphere4")
+    m = meshes.icosphere(4)
+    f = float(g["freq"])
+    o = Oracle(m)
+    assert o.n == 7680
+    for k, c in enumerate(g["cols"]):
+        assert rel(o.compute_matrix_cols(f, int(c), int(c) + 1)[:, 0], g["Zcols"][:, k]) < 1e-14, int(c)
+    V = o.rhs_plane_wave(f, 0.0, 0.0, 1.0, 0.0)
+    assert rel(V, g["V"]) < 1e-15
+    Z = o.compute_matrix(f)
+    assert rel(np.linalg.norm(Z, axis=0), g["colnorms"]) < 1e-14
+    assert abs(np.linalg.norm(Z) - float(g["fro"])) <= 1e-14 * float(g["fro"])
+    assert rel(o.solve(Z, V), g["I"]) < 1e-10
 
 
 def test_oracle_against_reference_build():
@@ -137,3 +161,31 @@ def test_gpu_sphere_golden(gpu_lib):
         s2 = Simulation(m, precision=prec)
         s2.run_context(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
         assert rel(s2.bistatic_rcs(10.0), g["bistatic"]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_gpu_sphere4_golden(gpu_lib):
+    """FRICO's own numbers at the benchmarked size, without the oracle: the FP64
+    drop-in's Z on the sampled columns (1e-10 of the entry, or 1e-14 of its term
+    magnitudes where its blocks cancel), its column norms and its currents against
+    FRICO's solve_general (1e-9), and the mixed path's currents (1e-6)."""
+    from frico_gb300.solver import PlaneWave, Simulation
+    g = load("sphere4")
+    m = meshes.icosphere(4)
+    f = float(g["freq"])
+    sim = Simulation(m, precision="fp64")
+    Z = sim.compute_matrix(f, download=True)
+    Zc = Z[:, g["cols"]]
+    excess = np.abs(Zc - g["Zcols"]) - (1e-10 * np.abs(g["Zcols"]) + 1e-14 * g["Mcols"])
+    assert excess.max() <= 0.0, excess.max()
+    assert rel(np.linalg.norm(Z, axis=0), g["colnorms"]) < 1e-12
+    del Z
+    sim.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+    assert rel(sim.get_rhs()[:, 0], g["V"]) < 1e-13
+    I = sim.solve()[:, 0]
+    assert np.linalg.norm(I - g["I"]) / np.linalg.norm(g["I"]) < 1e-9
+    mx = Simulation(m, precision="mixed")
+    mx.compute_matrix(f)
+    mx.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
+    Im = mx.solve()[:, 0]
+    assert np.linalg.norm(Im - g["I"]) / np.linalg.norm(g["I"]) < 1e-6
