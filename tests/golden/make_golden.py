@@ -19,6 +19,11 @@ Fixtures (all from FRICO's code, through oracle/ref/ref_driver.cpp):
                   (solve_general); with the oracle's term magnitudes of the sampled
                   columns (the tolerance scale where an entry's blocks cancel)
                   (`python tests/golden/make_golden.py sphere4`: about a minute)
+  bowtie1500.npz  the N ~ 1500 bowtie of the sweep at 500 MHz, delta-gap feed with
+                  FRICO's reorientation: 6 seeded columns of Z (with the oracle's
+                  term magnitudes), V, FRICO's I and port values, and kappa_1(Z)
+                  from LAPACK's zgecon (the scale of the solution's tolerance)
+                  (`python tests/golden/make_golden.py bowtie1500`)
 """
 from __future__ import annotations
 
@@ -51,6 +56,29 @@ def make_sphere4():
     np.savez_compressed(HERE / "sphere4.npz", freq=f, cols=cols, Zcols=np.ascontiguousarray(Z[:, cols]),
                         Mcols=M, colnorms=np.linalg.norm(Z, axis=0), fro=np.linalg.norm(Z), V=V, I=I)
     print("sphere4.npz", (HERE / "sphere4.npz").stat().st_size)
+
+
+def make_bowtie1500():
+    from oracle import Oracle
+    from scipy.linalg import lapack
+    f = 500e6
+    m = meshes.bowtie_preset(1500)
+    r = ref_frico.RefFrico(m)
+    signs = r.reorient([meshes.FEED_TAG])
+    Z = r.compute_matrix(f)
+    cols = np.sort(np.random.default_rng(20261205).choice(r.n, 6, replace=False))
+    V = r.rhs_delta_gap(f, [meshes.FEED_TAG])
+    I, _, _, _ = r.run_context_delta_gap(f, [meshes.FEED_TAG])
+    pv = r.port_values([meshes.FEED_TAG])
+    lu, _, _ = lapack.zgetrf(np.array(Z, order="F", copy=True))
+    rcond, _ = lapack.zgecon(lu, np.abs(Z).sum(axis=0).max(), norm="1")
+    M = np.stack([Oracle(m).compute_matrix_magnitudes(f, int(c), int(c) + 1)[:, 0] for c in cols], axis=1)
+    np.savez_compressed(HERE / "bowtie1500.npz", freq=f, reoriented=signs is not None,
+                        signs=signs if signs is not None else np.zeros(r.n),
+                        cols=cols, Zcols=np.ascontiguousarray(Z[:, cols]), Mcols=M, V=V, I=I,
+                        port=np.array([pv["current"], pv["power"], pv["impedance"], pv["gamma"], pv["swr"]]),
+                        kappa1=1.0 / rcond)
+    print("bowtie1500.npz", (HERE / "bowtie1500.npz").stat().st_size, "kappa_1 %.2e" % (1.0 / rcond))
 
 
 def main():
@@ -97,9 +125,9 @@ def main():
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["sphere4"]:
+    if sys.argv[1:] in (["sphere4"], ["bowtie1500"]):
         if not ref_frico.available():
             raise SystemExit("oracle/_ref/libfrico_ref.so missing: build it with oracle/ref/Makefile first")
-        make_sphere4()
+        make_sphere4() if sys.argv[1] == "sphere4" else make_bowtie1500()
     else:
         main()

@@ -94,11 +94,33 @@ def test_oracle_sphere4_golden():
     for k, c in enumerate(g["cols"]):
         assert rel(o.compute_matrix_cols(f, int(c), int(c) + 1)[:, 0], g["Zcols"][:, k]) < 1e-14, int(c)
     V = o.rhs_plane_wave(f, 0.0, 0.0, 1.0, 0.0)
-    assert rel(V, g["V"]) < 1e-15
+    assert rel(V, g["V"]) < 1e-14
     Z = o.compute_matrix(f)
     assert rel(np.linalg.norm(Z, axis=0), g["colnorms"]) < 1e-14
     assert abs(np.linalg.norm(Z) - float(g["fro"])) <= 1e-14 * float(g["fro"])
     assert rel(o.solve(Z, V), g["I"]) < 1e-10
+
+
+def test_oracle_bowtie1500_golden():
+    """The N ~ 1500 bowtie of the sweep at 500 MHz: the oracle's reorientation, sampled
+    Z columns and delta-gap V against FRICO's own code, and its LAPACK solve against
+    FRICO's solve_general within kappa_1 eps (kappa_1 = 4.8e8 here)."""
+    from oracle import Oracle
+    g = load("bowtie1500")
+    m = meshes.bowtie_preset(1500)
+    f = float(g["freq"])
+    o = Oracle(m)
+    s = o.reorient(FEED)
+    assert (s is not None) == bool(g["reoriented"])
+    if s is not None:
+        assert np.array_equal(s, g["signs"])
+    for k, c in enumerate(g["cols"]):
+        assert rel(o.compute_matrix_cols(f, int(c), int(c) + 1)[:, 0], g["Zcols"][:, k]) < 1e-14, int(c)
+    V = o.rhs_delta_gap(f, FEED, 1.0, s)
+    assert rel(V, g["V"]) < 1e-14
+    I = o.solve(o.compute_matrix(f), V)
+    eps = np.finfo(np.float64).eps
+    assert np.linalg.norm(I - g["I"]) / np.linalg.norm(g["I"]) < 10 * float(g["kappa1"]) * eps
 
 
 def test_oracle_against_reference_build():
@@ -189,3 +211,36 @@ def test_gpu_sphere4_golden(gpu_lib):
     mx.update_rhs(f, PlaneWave(0.0, 0.0, 1.0, 0.0))
     Im = mx.solve()[:, 0]
     assert np.linalg.norm(Im - g["I"]) / np.linalg.norm(g["I"]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_gpu_bowtie1500_golden(gpu_lib):
+    """FRICO's own numbers for the sweep's N ~ 1500 bowtie at 500 MHz, without the
+    oracle: the FP64 drop-in's Z on the sampled columns (1e-10 of the entry, or 1e-14
+    of its term magnitudes), and Zin and the currents of both paths against FRICO's
+    solve_general: Zin within max(tol, 1e-2 kappa_1 eps), the currents within
+    max(tol, 10 kappa_1 eps) (tol = 1e-9 FP64, 1e-6 mixed; kappa_1 = 4.8e8)."""
+    from frico_gb300.solver import DeltaGap, Simulation, reorient_deltagap_edges
+    g = load("bowtie1500")
+    m = meshes.bowtie_preset(1500)
+    f = float(g["freq"])
+    eps = np.finfo(np.float64).eps
+    kappa = float(g["kappa1"])
+    feed = DeltaGap((meshes.FEED_TAG,), 1.0)
+    zr = complex(g["port"][2])
+    for precision, tol in (("fp64", 1e-9), ("mixed", 1e-6)):
+        sim = Simulation(m, precision=precision)
+        sim.delta_gap_signs = reorient_deltagap_edges(sim.fs, feed.interfaces)
+        assert (sim.delta_gap_signs is not None) == bool(g["reoriented"])
+        if sim.delta_gap_signs is not None:
+            assert np.array_equal(np.asarray(sim.delta_gap_signs), g["signs"])
+        if precision == "fp64":
+            Z = sim.compute_matrix(f, download=True)
+            excess = np.abs(Z[:, g["cols"]] - g["Zcols"]) - (1e-10 * np.abs(g["Zcols"]) + 1e-14 * g["Mcols"])
+            assert excess.max() <= 0.0, excess.max()
+            del Z
+        I = sim.run_context(f, feed, download=True)[:, 0]
+        z = sim.port_values(feed)["impedance"]
+        sim.close()
+        assert abs(z - zr) < max(tol, 1e-2 * kappa * eps) * abs(zr), (precision, z, zr)
+        assert np.linalg.norm(I - g["I"]) / np.linalg.norm(g["I"]) < max(tol, 10 * kappa * eps), precision
