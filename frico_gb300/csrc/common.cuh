@@ -267,7 +267,7 @@ struct StageTimer {
 // the first time (device, key) is seen in this process and returns its status;
 // a failed init runs again on the next call. Safe to call from several host
 // threads (each driving its own context).
-enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceTrsv128, kOnceGemmDf, kOnceKeys };
+enum OnceKey { kOnceDunavant = 0, kOnceGemmTc, kOnceNopivLu, kOnceTrsmLower, kOnceTrsv128, kOnceGemmDf, kOnceGemmPair, kOnceKeys };
 int device_once(frico_gpu_ctx* ctx, OnceKey key, int (*init)(frico_gpu_ctx*));
 
 // Limit of the device-side waits on other CTAs (chained solves, grid barrier), in SM cycles.

@@ -46,6 +46,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -514,6 +515,267 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_f16x3(
     gemm_body<BN, true>(tmAh0, tmAl0, tmBh0, tmBl0, tmAh1, tmAl1, tmBh1, tmBl1, g);
 }
 
+// ---- the trailing update on SM pairs (cta_group::2).
+// The one-CTA kernel above is bound by the TMA operand feed from L2: per 128 x 128
+// tile and 32-float K slab it loads 64 KB of operands for 128 x 128 x 32 x 3 MMA
+// multiply-adds. Here the two CTAs of a cluster share one 256 x 256 tile: each loads
+// its own 128 rows of A* and 128 rows of B^ (the same 64 KB per slab), and the even
+// CTA's MMA warp issues M = 256, N = 256 tcgen05.mma (cta_group::2) over both CTAs'
+// shared memory, so every CTA's slab feeds twice the multiply-adds. Each CTA's TMEM
+// holds its own 128 rows x 256 columns (two accumulators in rotation); its eight
+// epilogue warps update its half of the tile as above (no operand emission here).
+// Hand-offs: both CTAs' TMA loads complete on the even CTA's full barrier (which
+// expects both CTAs' bytes); its commits arrive on both CTAs' empty and tfull
+// barriers (multicast); every epilogue warp of both CTAs arrives on the even CTA's
+// tempty barrier. All waits are bounded as above.
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// The shared::cluster address of the same shared-memory object in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa_rank(const void* p, uint32_t rank) {
+    uint32_t a;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(p)), "r"(rank));
+    return a;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint32_t bar_cluster, int x,
+                                                 int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+        "%4}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(x), "r"(y)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_pair_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_pair_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                             uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+// arrive on the barrier at the same offset in both CTAs of the pair when the MMAs issued so far are done
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"((unsigned short)3)
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+
+static const int kPairAccs = 2;   // 256-column accumulators in rotation (all 512 TMEM columns)
+
+template <bool H>
+__device__ __forceinline__ void gemm_pair_body(const CUtensorMap& tmAh, const CUtensorMap& tmAl,
+                                               const CUtensorMap& tmBh, const CUtensorMap& tmBl, const GemmArgs& g) {
+    constexpr int STAGES = Cfg<128>::STAGES, STAGE_BYTES = Cfg<128>::STAGE_BYTES;
+    constexpr int A_TILE = Cfg<128>::A_TILE, B_TILE = Cfg<128>::B_TILE;
+    constexpr int BKE = H ? 2 * BK : BK;
+    constexpr int PM = 2 * BM, PN = 256;   // the pair's tile
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char* ring = (unsigned char*)((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
+    uint64_t* bars = (uint64_t*)(ring + STAGES * STAGE_BYTES);
+    uint64_t* full = bars;                        // [STAGES], used in the even CTA
+    uint64_t* empty = bars + STAGES;              // [STAGES]
+    uint64_t* tfull = bars + 2 * STAGES;          // [kPairAccs]
+    uint64_t* tempty = tfull + kPairAccs;         // [kPairAccs], used in the even CTA
+    uint32_t* tmem_slot = (uint32_t*)(tempty + kPairAccs);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_rank();
+    const GemmProb& P = g.p[0];
+    const int tm2 = (P.M + PM - 1) / PM, ntp = tm2 * ((P.N + PN - 1) / PN);
+    const int cid = int(blockIdx.x >> 1), ncl = int(gridDim.x >> 1);
+    const int kslabs = g.KP / BKE;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < kPairAccs; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 2 * kEpiWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {   // one warp of each CTA of the pair, collectively
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    cluster_sync_all();   // both CTAs' barriers initialised before any remote arrival
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int t = cid; t < ntp && ok; t += ncl) {
+                const int mt = t % tm2, nt_ = t / tm2;
+                for (int ks = 0; ks < kslabs; ks++, it++) {
+                    const int s = it % STAGES, round = it / STAGES;
+                    if (!(ok = mbar_wait(&empty[s], (round & 1) ^ 1, g.st))) break;
+                    unsigned char* base = ring + s * STAGE_BYTES;
+                    if (rank == 0) mbar_expect_tx(&full[s], 2 * STAGE_BYTES);
+                    const uint32_t fb = mapa_rank(&full[s], 0);
+                    const int ya = mt * PM + int(rank) * BM, yb = nt_ * PN + int(rank) * 128;
+                    tma_load_2d_pair(base, &tmAh, fb, ks * BKE, ya);
+                    tma_load_2d_pair(base + A_TILE, &tmAl, fb, ks * BKE, ya);
+                    tma_load_2d_pair(base + 2 * A_TILE, &tmBh, fb, ks * BKE, yb);
+                    tma_load_2d_pair(base + 2 * A_TILE + B_TILE, &tmBl, fb, ks * BKE, yb);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {
+            const uint32_t idesc = H ? idesc_f16(PM, PN) : idesc_tf32(PM, PN);
+            int it = 0, tcount = 0;
+            bool ok = true;
+            for (int t = cid; t < ntp && ok; t += ncl, tcount++) {
+                const int acc = tcount % kPairAccs, around = tcount / kPairAccs;
+                if (!(ok = mbar_wait(&tempty[acc], (around & 1) ^ 1, g.st))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t tmem_d = tmem_base + uint32_t(acc * PN);
+                for (int ks = 0; ks < kslabs; ks++, it++) {
+                    const int s = it % STAGES, round = it / STAGES;
+                    if (!(ok = mbar_wait(&full[s], round & 1, g.st))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t base = smem_u32(ring + s * STAGE_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint32_t off = uint32_t(kk * 32);
+                        const uint64_t ah = smem_desc_sw128(base + off);
+                        const uint64_t al = smem_desc_sw128(base + A_TILE + off);
+                        const uint64_t bh = smem_desc_sw128(base + 2 * A_TILE + off);
+                        const uint64_t bl = smem_desc_sw128(base + 2 * A_TILE + B_TILE + off);
+                        const uint32_t first = (ks == 0 && kk == 0) ? 0u : 1u;
+                        if constexpr (H) {
+                            mma_pair_f16(tmem_d, ah, bh, idesc, first);
+                            mma_pair_f16(tmem_d, ah, bl, idesc, 1u);
+                            mma_pair_f16(tmem_d, al, bh, idesc, 1u);
+                        } else {
+                            mma_pair_tf32(tmem_d, ah, bh, idesc, first);
+                            mma_pair_tf32(tmem_d, ah, bl, idesc, 1u);
+                            mma_pair_tf32(tmem_d, al, bh, idesc, 1u);
+                        }
+                    }
+                    mma_commit_pair(&empty[s]);
+                }
+                if (!ok) break;
+                mma_commit_pair(&tfull[acc]);
+            }
+        }
+    } else {
+        // epilogue warps 2..9: TMEM lane quadrant q, columns [128 h2, 128 h2 + 128) in two halves
+        const int q = warp & 3, h2 = ((warp - 2) >> 2) * 128;
+        const int row = q * 32 + lane;
+        const int64_t ldc = P.ldc;
+        const int accumulate = P.accumulate;
+        float osc = 1.f;
+        if constexpr (H) osc = pow_scale(P.osp, P.oc, P.op);
+        int tcount = 0;
+        for (int t = cid; t < ntp; t += ncl, tcount++) {
+            const int acc = tcount % kPairAccs, around = tcount / kPairAccs;
+            const int mt = t % tm2, nt_ = t / tm2;
+            const int gr = mt * PM + int(rank) * BM + row;
+            const bool rowok = gr < P.M;
+            if (kPrefetchC && accumulate) {   // the next tile's C lines of this warp into L2
+                const int tq = t + ncl;
+                if (tq < ntp) {
+                    const int mq = tq % tm2, nq = tq / tm2, r0 = mq * PM + int(rank) * BM + q * 32;
+                    if (r0 < P.M) {
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const int col = nq * PN + h2 + lane + 32 * k;
+                            if (col < P.N) asm volatile("prefetch.global.L2 [%0];" ::"l"(P.C + int64_t(col) * ldc + r0));
+                        }
+                    }
+                }
+            }
+            bool ready = true;
+#pragma unroll 1
+            for (int hh = 0; hh < 128; hh += 64) {
+                const int c0 = nt_ * PN + h2 + hh;
+                const int ncol = min(64, P.N - c0);
+                float* cp = P.C + int64_t(c0) * ldc + gr;
+                float cv[64];
+                if (accumulate && rowok && ncol == 64) {
+#pragma unroll
+                    for (int j = 0; j < 64; j++) cv[j] = cp[int64_t(j) * ldc];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 64; j++) cv[j] = (accumulate && rowok && j < ncol) ? cp[int64_t(j) * ldc] : 0.f;
+                }
+                if (hh == 0) {
+                    if (!(ready = mbar_wait(&tfull[acc], around & 1, g.st))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                }
+                const uint32_t taddr = tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * PN + h2 + hh);
+                float* sp;
+                asm volatile("mov.b64 %0, %1;" : "=l"(sp) : "l"(cp));
+#pragma unroll
+                for (int c1 = 0; c1 < 64; c1 += 32) {
+                    float v[32];
+                    tmem_ld32(taddr + uint32_t(c1), v);
+                    float* wp = sp + int64_t(c1) * ldc;
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const float d = H ? v[j] * osc : v[j];
+                        if (rowok && c1 + j < ncol) wp[int64_t(j) * ldc] = accumulate ? cv[c1 + j] - d : d;
+                    }
+                }
+            }
+            if (!ready) break;
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(mapa_rank(&tempty[acc], 0));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    cluster_sync_all();   // no CTA leaves while its peer may still signal its barriers or read its TMEM
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512));
+    }
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+    k_gemm_pair_tf32x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                       const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+                       const __grid_constant__ GemmArgs g) {
+    gemm_pair_body<false>(tmAh, tmAl, tmBh, tmBl, g);
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+    k_gemm_pair_f16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                      const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+                      const __grid_constant__ GemmArgs g) {
+    gemm_pair_body<true>(tmAh, tmAl, tmBh, tmBl, g);
+}
+
 // ---- products whose sums must stay beyond FP32 accuracy (the far field, fields_gemm.cu).
 // The tensor cores accumulate in FP32 with a rounding of the running sum at every MMA,
 // which over the hundreds of MMAs of a long K loses several digits (about 1e-6 relative
@@ -940,6 +1202,53 @@ static int make_problem(frico_gpu_ctx* ctx, TcProblem& q, float2* C, int64_t ldc
     return FRICO_GPU_OK;
 }
 
+// Trailing updates without operand emission and more than 128 columns run on SM pairs
+// (k_gemm_pair_*); the most clusters of two that the device keeps resident at once.
+static const bool kPairGemm = true;
+static std::atomic<int> g_pair_clusters[64];
+
+static int launch_gemm_pair(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem& q, int KP, int cap,
+                            cudaEvent_t* ev) {
+    int rc;
+    if ((rc = device_once(ctx, kOnceGemmPair, [](frico_gpu_ctx* c) {
+             const void* fns[2] = {(const void*)tc::k_gemm_pair_tf32x3, (const void*)tc::k_gemm_pair_f16x3};
+             int most = 1 << 30;
+             for (const void* f : fns) {
+                 int r = cuda_check(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                            tc::Cfg<128>::SMEM_BYTES), "pair smem attribute");
+                 if (r) return r;
+                 cudaLaunchConfig_t cfg = {};
+                 cfg.gridDim = dim3(2, 1, 1);
+                 cfg.blockDim = dim3(tc::kThreads, 1, 1);
+                 cfg.dynamicSmemBytes = tc::Cfg<128>::SMEM_BYTES;
+                 int nc = 0;
+                 if ((r = cuda_check(c, cudaOccupancyMaxActiveClusters(&nc, f, &cfg), "pair occupancy"))) return r;
+                 most = std::min(most, nc);
+             }
+             if (most < 1) return set_err(c, FRICO_GPU_ECUDA, "no SM pair can hold the pair GEMM");
+             g_pair_clusters[c->device & 63] = most;
+             return FRICO_GPU_OK;
+         })))
+        return rc;
+    const tc::GemmProb& P = q.p;
+    const int ntp = ((P.M + 2 * tc::BM - 1) / (2 * tc::BM)) * ((P.N + 255) / 256);
+    const int ncl = std::max(1, std::min({ntp, cap / 2, g_pair_clusters[ctx->device & 63].load()}));
+    tc::GemmArgs ga;
+    ga.p[0] = P;
+    ga.p[1] = P;
+    ga.nprob = 1;
+    ga.KP = KP;
+    ga.st = (DeviceStatus*)ctx->status.p;
+    if (ev) cudaEventRecord(ev[0], st);
+    if (q.h)
+        tc::k_gemm_pair_f16x3<<<2 * ncl, tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(q.mah, q.mal, q.mbh, q.mbl, ga);
+    else
+        tc::k_gemm_pair_tf32x3<<<2 * ncl, tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(q.mah, q.mal, q.mbh, q.mbl, ga);
+    if (ev) cudaEventRecord(ev[1], st);
+    count_launch(ctx);
+    return cuda_check(ctx, cudaGetLastError(), q.h ? "k_gemm_pair_f16x3" : "k_gemm_pair_tf32x3");
+}
+
 static int launch_gemm(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem* q, int np, int KP, int max_ctas,
                        cudaEvent_t* ev) {
     int rc;
@@ -956,6 +1265,9 @@ static int launch_gemm(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem* q, 
     if (np > 1 && q[0].h != q[1].h) return set_err(ctx, FRICO_GPU_EINVAL, "launch_gemm: mixed operand types");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
+    if (kPairGemm && np == 1 && q[0].p.emit == 0 && q[0].p.N > 128 && q[0].p.M > tc::BM && cap >= 2)
+        return launch_gemm_pair(ctx, st, q[0], KP, cap, ev);
     tc::GemmArgs ga;
     ga.p[0] = q[0].p;
     ga.p[1] = q[np > 1 ? 1 : 0].p;
@@ -966,7 +1278,6 @@ static int launch_gemm(frico_gpu_ctx* ctx, cudaStream_t st, const TcProblem* q, 
     if (ntiles == 0) return FRICO_GPU_OK;
     const TcProblem& q1 = q[np > 1 ? 1 : 0];
     if (ev) cudaEventRecord(ev[0], st);
-    const int cap = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
     if (q[0].h)
         tc::k_gemm_f16x3<128><<<std::min(ntiles, cap), tc::kThreads, tc::Cfg<128>::SMEM_BYTES, st>>>(
             q[0].mah, q[0].mal, q[0].mbh, q[0].mbl, q1.mah, q1.mal, q1.mbh, q1.mbl, ga);
