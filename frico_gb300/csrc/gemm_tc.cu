@@ -584,6 +584,22 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
 }
 
 static const int kPairAccs = 2;   // 256-column accumulators in rotation (all 512 TMEM columns)
+static const bool kPairPrefetchC = true;
+static const int kPairGroup = 8;   // > 0: tiles walk M within groups of this many tile columns (measured best of 0, 4, 8, 16)
+
+// Tile t of the pair grid (tm2 x tn2 tiles of 256 x 256): M first, or M first within
+// groups of kPairGroup tile columns.
+__device__ __forceinline__ void pair_tile(int t, int tm2, int tn2, int& mt, int& nt) {
+    if (kPairGroup > 0) {
+        const int per = tm2 * kPairGroup, gi = t / per, r = t - gi * per;
+        const int gw = min(kPairGroup, tn2 - gi * kPairGroup);
+        mt = r / gw;
+        nt = gi * kPairGroup + r % gw;
+    } else {
+        mt = t % tm2;
+        nt = t / tm2;
+    }
+}
 
 template <bool H>
 __device__ __forceinline__ void gemm_pair_body(const CUtensorMap& tmAh, const CUtensorMap& tmAl,
@@ -604,7 +620,7 @@ __device__ __forceinline__ void gemm_pair_body(const CUtensorMap& tmAh, const CU
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t rank = cluster_rank();
     const GemmProb& P = g.p[0];
-    const int tm2 = (P.M + PM - 1) / PM, ntp = tm2 * ((P.N + PN - 1) / PN);
+    const int tm2 = (P.M + PM - 1) / PM, tn2 = (P.N + PN - 1) / PN, ntp = tm2 * tn2;
     const int cid = int(blockIdx.x >> 1), ncl = int(gridDim.x >> 1);
     const int kslabs = g.KP / BKE;
 
@@ -634,7 +650,8 @@ __device__ __forceinline__ void gemm_pair_body(const CUtensorMap& tmAh, const CU
             int it = 0;
             bool ok = true;
             for (int t = cid; t < ntp && ok; t += ncl) {
-                const int mt = t % tm2, nt_ = t / tm2;
+                int mt, nt_;
+                pair_tile(t, tm2, tn2, mt, nt_);
                 for (int ks = 0; ks < kslabs; ks++, it++) {
                     const int s = it % STAGES, round = it / STAGES;
                     if (!(ok = mbar_wait(&empty[s], (round & 1) ^ 1, g.st))) break;
@@ -699,13 +716,16 @@ __device__ __forceinline__ void gemm_pair_body(const CUtensorMap& tmAh, const CU
         int tcount = 0;
         for (int t = cid; t < ntp; t += ncl, tcount++) {
             const int acc = tcount % kPairAccs, around = tcount / kPairAccs;
-            const int mt = t % tm2, nt_ = t / tm2;
+            int mt, nt_;
+            pair_tile(t, tm2, tn2, mt, nt_);
             const int gr = mt * PM + int(rank) * BM + row;
             const bool rowok = gr < P.M;
-            if (kPrefetchC && accumulate) {   // the next tile's C lines of this warp into L2
+            if (kPairPrefetchC && accumulate) {   // the next tile's C lines of this warp into L2
                 const int tq = t + ncl;
                 if (tq < ntp) {
-                    const int mq = tq % tm2, nq = tq / tm2, r0 = mq * PM + int(rank) * BM + q * 32;
+                    int mq, nq;
+                    pair_tile(tq, tm2, tn2, mq, nq);
+                    const int r0 = mq * PM + int(rank) * BM + q * 32;
                     if (r0 < P.M) {
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
