@@ -138,9 +138,10 @@ def measured_peaks():
 
 
 # DRAM traffic (ncu: dram__bytes_read.sum + dram__bytes_write.sum) per launch of the complex64
-# LU's narrow and trailing-update GEMMs, averaged over every update launch of one L4-sphere
-# solve; the capture and its command are summarised in profiles/k_gemm_tf32x3_sphere_L4_mixed.md.
-GEMM_TRAFFIC_BYTES_PER_LAUNCH = {("k_gemm_tf32x3", 4): 157.3e6}
+# LU's narrow (k_gemm_tf32x3) and trailing-update (k_gemm_pair_tf32x3) GEMMs, averaged over
+# the 116 update launches of one L4-sphere solve; the capture and its command are summarised
+# in profiles/launch_list_sphere_L4_mixed.md.
+GEMM_TRAFFIC_BYTES_PER_LAUNCH = {("k_gemm_pair_tf32x3 + k_gemm_tf32x3", 4): 182.5e6}
 
 
 def gemm_traffic_per_launch(level: int, precision: str, kernel: str):
@@ -413,7 +414,9 @@ def run_ours(args):
     tc = args.precision == "mixed" and args.gemm_engine != "simt"
     # the unpivoted LU's block columns run 3xFP16 when asked for; everything else 3xTF32
     f16 = tc and args.gemm_engine == "tc_f16" and s1["pivoting_used"] == 2
-    kernel = ("tc::k_gemm_f16x3" if f16 else "tc::k_gemm_tf32x3") if tc else "k_gemm_update<float>"
+    # trailing updates on SM pairs, the narrow update of the next block column on single SMs
+    kernel = (("tc::k_gemm_pair_f16x3 + tc::k_gemm_f16x3" if f16 else "tc::k_gemm_pair_tf32x3 + tc::k_gemm_tf32x3")
+              if tc else "k_gemm_update<float>")
     # tensor work of the split path: 3 real GEMMs of (2m x 2k)(2k x n) = 3 x algorithmic complex flops;
     # FP16 dense peak = the measured dense bf16 peak, TF32 = half of it
     tflops_alg = gfl / sec / 1e12
