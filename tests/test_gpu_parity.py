@@ -519,8 +519,18 @@ def test_mixed_ill_conditioned_refines_with_gmres(gpu_lib, residual):
     assert st["precision_used"] == 1, st
     assert st["refine_iters"] > 6, st   # GMRES, not classical refinement alone
     assert st["refine_residual"] <= 1e-12
-    true = np.linalg.norm(B[:, 0] - Z @ I[:, 0]) / np.linalg.norm(B[:, 0])
-    assert true <= 1e-12, true
+    # At this size and frequency || |Z| |I| || / ||B|| = 1.3e4: an FP64 evaluation of the
+    # residual carries noise of a few eps times that (LAPACK's own FP64 solve of this system
+    # measures 1.7e-12; a 1e-16 relative change of I moves the residual by 3%), so the library's
+    # FP64 residual and any other agree only to about 10% at 1e-12. Here the residual of the
+    # returned currents is evaluated in extended precision and held to the tolerance plus
+    # u || |Z| |I| || / ||B|| (u = eps / 2, 1.4e-12 here), the first-order noise of the FP64
+    # evaluation that decided convergence.
+    Zl, Il, Bl = Z.astype(np.clongdouble), I[:, 0].astype(np.clongdouble), B[:, 0].astype(np.clongdouble)
+    bn = np.linalg.norm(B[:, 0])
+    true = float(np.sqrt(np.sum(np.abs(Bl - Zl @ Il) ** 2))) / bn
+    noise = 0.5 * np.finfo(np.float64).eps * np.linalg.norm(np.abs(Z) @ np.abs(I[:, 0])) / bn
+    assert true <= 1e-12 + noise, (true, noise)
     assert rel_norm(I, Ir) < 1e-8
 
 
