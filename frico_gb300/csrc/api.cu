@@ -155,6 +155,7 @@ extern "C" int frico_gpu_ctx_destroy(frico_gpu_ctx* ctx) {
                       &ctx->dinv128, &ctx->trsv_x, &ctx->ffws};
     for (DevBuf* b : bufs) release(*b);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
@@ -241,24 +242,47 @@ extern "C" int frico_gpu_set_mesh(frico_gpu_ctx* ctx, int64_t nv, const double* 
             tri_old[next++] = int32_t(t);
         }
     int rc;
-    auto up = [&](DevBuf& b, const void* src, size_t bytes) -> int {
-        int r = ensure(ctx, b, bytes);
-        if (r) return r;
-        return cuda_check(ctx, cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice), "upload");
+    // all arrays through one pinned staging buffer: asynchronous copies on the context's
+    // stream, then one synchronisation (the data is on the device when this returns)
+    struct Up {
+        DevBuf* b;
+        const void* src;
+        size_t bytes;
     };
-    if ((rc = up(ctx->xyz, xyz, sizeof(double) * 3 * nv))) return rc;
-    if ((rc = up(ctx->tri, tri, sizeof(int64_t) * 3 * nt))) return rc;
-    if ((rc = up(ctx->rwg_itm, itm.data(), sizeof(int32_t) * n))) return rc;
-    if ((rc = up(ctx->rwg_itp, itp.data(), sizeof(int32_t) * n))) return rc;
-    if ((rc = up(ctx->rwg_itf, itf.data(), sizeof(int32_t) * n))) return rc;
-    if ((rc = up(ctx->rwg_len, len.data(), sizeof(double) * n))) return rc;
-    if ((rc = up(ctx->rwg_am, am.data(), sizeof(double) * n))) return rc;
-    if ((rc = up(ctx->rwg_ap, ap.data(), sizeof(double) * n))) return rc;
-    if ((rc = up(ctx->rwg_vm, vm.data(), sizeof(double) * 3 * n))) return rc;
-    if ((rc = up(ctx->rwg_vp, vp.data(), sizeof(double) * 3 * n))) return rc;
-    if ((rc = up(ctx->tri_bf, tri_bf.data(), sizeof(int32_t) * 3 * nt))) return rc;
-    if ((rc = up(ctx->tri_new, tri_new.data(), sizeof(int32_t) * nt))) return rc;
-    if ((rc = up(ctx->tri_old, tri_old.data(), sizeof(int32_t) * nt))) return rc;
+    const Up ups[] = {{&ctx->xyz, xyz, sizeof(double) * 3 * nv},
+                      {&ctx->tri, tri, sizeof(int64_t) * 3 * nt},
+                      {&ctx->rwg_itm, itm.data(), sizeof(int32_t) * n},
+                      {&ctx->rwg_itp, itp.data(), sizeof(int32_t) * n},
+                      {&ctx->rwg_itf, itf.data(), sizeof(int32_t) * n},
+                      {&ctx->rwg_len, len.data(), sizeof(double) * n},
+                      {&ctx->rwg_am, am.data(), sizeof(double) * n},
+                      {&ctx->rwg_ap, ap.data(), sizeof(double) * n},
+                      {&ctx->rwg_vm, vm.data(), sizeof(double) * 3 * n},
+                      {&ctx->rwg_vp, vp.data(), sizeof(double) * 3 * n},
+                      {&ctx->tri_bf, tri_bf.data(), sizeof(int32_t) * 3 * nt},
+                      {&ctx->tri_new, tri_new.data(), sizeof(int32_t) * nt},
+                      {&ctx->tri_old, tri_old.data(), sizeof(int32_t) * nt}};
+    size_t total = 0;
+    for (const Up& u : ups) total += (u.bytes + 255) & ~size_t(255);
+    // the previous upload from the staging buffer has finished: its call synchronised
+    if (total > ctx->h_stage_bytes) {
+        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        ctx->h_stage = nullptr;
+        ctx->h_stage_bytes = 0;
+        if ((rc = cuda_check(ctx, cudaHostAlloc(&ctx->h_stage, total, cudaHostAllocDefault), "pinned staging")))
+            return rc;
+        ctx->h_stage_bytes = total;
+    }
+    size_t off = 0;
+    for (const Up& u : ups) {
+        if ((rc = ensure(ctx, *u.b, u.bytes))) return rc;
+        char* h = (char*)ctx->h_stage + off;
+        std::memcpy(h, u.src, u.bytes);
+        if ((rc = cuda_check(ctx, cudaMemcpyAsync(u.b->p, h, u.bytes, cudaMemcpyHostToDevice, ctx->stream), "upload")))
+            return rc;
+        off += (u.bytes + 255) & ~size_t(255);
+    }
+    if ((rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "upload sync"))) return rc;
     ctx->nv = nv;
     ctx->nt = nt;
     ctx->n = n;

@@ -189,6 +189,8 @@ struct frico_gpu_ctx {
     // of RWG pairs lie in a small block of it
     frico::DevBuf tri_new;        // [nt] new number of each triangle
     frico::DevBuf tri_old;        // [nt] triangle of each new number
+    void* h_stage = nullptr;      // pinned host staging of the mesh upload (frico_gpu_set_mesh)
+    size_t h_stage_bytes = 0;
     std::vector<frico_rwg> h_rwg; // host copy (port values, interfaces)
     std::vector<double> h_xyz;    // host copies of the mesh (sweep lanes are built from them)
     std::vector<int64_t> h_tri;
