@@ -330,7 +330,9 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
             for (int cc = 0; cc < 32; cc++) lv[cc] = (r < bs && q * 32 + cc < cs) ? col[int64_t(cc) * lda] : z;
         }
     };
-    // x of block column cb into xs[buf] once every value of it is final (warp 0; bounded wait)
+    // x of block column cb into xs[buf] once every value of it is final (warp 0; bounded wait).
+    // Per right-hand side a lane issues its 4 loads before it checks any, so that they cost
+    // one L2 round trip rather than four.
     auto await_x = [&](int cb, int buf) {
         if (warp == 0) {
             const int c0 = cb * kB2, cs = min(kB2, n - c0);
@@ -338,14 +340,20 @@ __global__ void __launch_bounds__(512) k_trsv_chain128(const float2* __restrict_
             volatile int* e = &st->err;
             while (true) {
                 bool pending = false;
-                for (int idx = lane; idx < kB2 * nrhs; idx += 32) {
-                    const int rr = idx & (kB2 - 1), c = idx >> 7;
-                    float2 v = z;
-                    if (rr < cs) {
-                        v = ld_relaxed_f2(&Xout[int64_t(c) * ldout + c0 + rr]);
-                        pending |= __float_as_uint(v.x) == kUnset || __float_as_uint(v.y) == kUnset;
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    if (NC > 1 && c >= nrhs) break;
+                    float2 v[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const int rr = lane + 32 * i;
+                        v[i] = rr < cs ? ld_relaxed_f2(&Xout[int64_t(c) * ldout + c0 + rr]) : z;
                     }
-                    xs[buf][rr][c] = v;
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        pending |= __float_as_uint(v[i].x) == kUnset || __float_as_uint(v[i].y) == kUnset;
+                        xs[buf][lane + 32 * i][c] = v[i];
+                    }
                 }
                 if (!__any_sync(0xffffffffu, pending)) break;
                 if (lane == 0 && (*e || clock64() - t0 > lim)) {
