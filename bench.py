@@ -141,7 +141,7 @@ def measured_peaks():
 # LU's narrow (k_gemm_tf32x3) and trailing-update (k_gemm_pair_tf32x3) GEMMs, averaged over
 # the 116 update launches of one L4-sphere solve; the capture and its command are summarised
 # in profiles/launch_list_sphere_L4_mixed.md.
-GEMM_TRAFFIC_BYTES_PER_LAUNCH = {("k_gemm_pair_tf32x3 + k_gemm_tf32x3", 4): 182.5e6}
+GEMM_TRAFFIC_BYTES_PER_LAUNCH = {("k_gemm_pair_tf32x3 + k_gemm_tf32x3", 4): 177.3e6}
 
 
 def gemm_traffic_per_launch(level: int, precision: str, kernel: str):
