@@ -549,12 +549,22 @@ __global__ void __launch_bounds__(256) k_residual_part(const double2* __restrict
 // finite) sets st->df_range; the caller then recomputes with k_residual_part.
 // (split_df, df_mac and df_renorm are in common.cuh.)
 // NC right-hand sides per pass (1, 2, 4 or 8: register use grows with NC);
-// 8 entries of Z are loaded ahead of their use.
+// 8 entries of Z are loaded ahead of their use. Of every 8 entries, the last
+// kResidualF64<NC> go through the FP64 pipe instead (four DFMAs into the FP64
+// sum), which the double-float arithmetic leaves idle: a DFMA warp-instruction
+// takes about 80 cycles of a sub-partition's FP64 pipe on this part, a
+// double-float product about 12 issue slots, so the two finish together near
+// 2 of 8 entries for one right-hand side and 1 of 8 for eight (the split of Z
+// is shared by the right-hand sides, the DFMAs are not).
+template <int NC> constexpr int kResidualF64 = NC <= 2 ? 2 : 1;
+
 template <int NC>
 __global__ void __launch_bounds__(256) k_residual_part_df(const double2* __restrict__ Z, int64_t ldz, int n,
                                                          const double2* __restrict__ X, int64_t ld, int nrhs,
                                                          int chunk, double2* __restrict__ part, DeviceStatus* st) {
+    constexpr int F64 = kResidualF64<NC>, DF = 8 - F64;   // entries per 8 through FP64 / double-float
     __shared__ float4 xs[128 * NC];   // (re hi, re lo, im hi, im lo) of X[i0 + ii, c0 + c]
+    __shared__ double2 xd[128 * NC];  // the same in FP64
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
     int bad = 0;
@@ -577,6 +587,7 @@ __global__ void __launch_bounds__(256) k_residual_part_df(const double2* __restr
                 split_df(x.x, q.x, q.y, bad);
                 split_df(x.y, q.z, q.w, bad);
                 xs[c * 128 + ii] = q;
+                xd[c * 128 + ii] = x;
             }
             __syncthreads();
             if (r < n) {
@@ -593,6 +604,12 @@ __global__ void __launch_bounds__(256) k_residual_part_df(const double2* __restr
 #pragma unroll
                         for (int u = 0; u < 8; u++) {
                             if (ii + u >= be) break;
+                            if (u >= DF) {   // FP64 pipe
+#pragma unroll
+                                for (int c = 0; c < NC; c++)
+                                    if (NC == 1 || c < nc) cmac(acc[c], zz[u], xd[c * 128 + ii + u]);
+                                continue;
+                            }
                             float zr1, zr2, zi1, zi2;
                             split_df(zz[u].x, zr1, zr2, bad);
                             split_df(zz[u].y, zi1, zi2, bad);
@@ -604,7 +621,7 @@ __global__ void __launch_bounds__(256) k_residual_part_df(const double2* __restr
                                     df_mac(sr[c], tr[c], -zi1, -zi2, x.z, x.w);
                                     df_mac(si[c], ti[c], zr1, zr2, x.z, x.w);     // Im += zr xi + zi xr
                                     df_mac(si[c], ti[c], zi1, zi2, x.x, x.y);
-                                    if (u == 3 || u == 7) {
+                                    if (u == 3 || u == DF - 1) {
                                         df_renorm(sr[c], tr[c]);
                                         df_renorm(si[c], ti[c]);
                                     }
