@@ -41,6 +41,9 @@
 //               overlaps the tile's MMAs; then tcgen05.ld, C -= D, stores.
 // All mbarrier waits are bounded; on timeout the CTA records
 // FRICO_DEV_ERR_TIMEOUT in the status word and leaves its loops.
+// Trailing updates without operand emission and wider than 128 columns run on
+// SM pairs instead (k_gemm_pair_*: 256 x 256 tiles per cluster of two CTAs,
+// tcgen05.mma.cta_group::2), which halves the operand bytes per multiply-add.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
